@@ -1,0 +1,126 @@
+/*
+ * pelelm_gb300 — GB300-native (sm_103a) replacement of the PelePhysics chemistry reactor that
+ * PeleLM drives from PeleLM::advance_chemistry (Source/PeleLM.cpp:5626-5845).
+ *
+ * Plain C ABI: plain pointers and sizes, no C++ or framework types. All device pointers are
+ * CUDA device (or managed) memory owned by the caller; the library only reads and writes
+ * them in place. Units inside the reactor are CGS, exactly as the reference passes them
+ * (rhoY g/cm^3, rhoH erg/cm^3, T K, forcing per second) — Source/PeleLM.cpp:5736-5746.
+ *
+ * Every entry point returns 0 (or a non-negative count) on success and a negative value on a
+ * usage / CUDA error; pgb_last_error() then describes it. Nothing throws across the ABI and no
+ * device code traps.
+ */
+#ifndef PELELM_GB300_H
+#define PELELM_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PGB_ABI_VERSION 1
+
+typedef struct pgb_reactor pgb_reactor;
+
+/* Mirror of amrex::Array4<T>: element (i,j,k,n) is
+ * p[(i-begin[0]) + (j-begin[1])*jstride + (k-begin[2])*kstride + n*nstride]. */
+typedef struct {
+  void* p;
+  long long jstride, kstride, nstride;
+  int begin[3];
+  int end[3]; /* exclusive, as amrex::Array4::end */
+  int ncomp;
+} pgb_array4;
+
+/* Mirror of amrex::Box (cell-centred, inclusive smallEnd/bigEnd). */
+typedef struct {
+  int lo[3];
+  int hi[3];
+} pgb_box;
+
+/* The arguments of ReactorBase::react for one box (Source/PeleLM.cpp:5752-5757):
+ * rY (NUM_SPECIES comps), rY_src (NUM_SPECIES), T, rEner (rho h), rEner_src, FC, mask.
+ * mask.p may be NULL (all cells react); mask < 0 marks covered cells, which are skipped
+ * (their FC is set to 0), the Source/PeleLM_K.H:66-72 convention. */
+typedef struct {
+  pgb_box box;
+  pgb_array4 rY, rY_src, T, rEner, rEner_src, FC, mask;
+} pgb_box_view;
+
+/* Counters of the last advance (pgb_reactor_get_stats). hist[b] counts cells whose BDF step
+ * count lies in [2^b, 2^(b+1)). */
+typedef struct {
+  unsigned long long ncell, nst, nfe, nje, netf, ncfn, nfail, max_nst;
+  unsigned long long hist[16];
+} pgb_stats;
+
+/* ReactorBase::create(name) followed by init(reactor_type, ncells)
+ * (Source/PeleLM.cpp:706-709). name: "ReactorCvode" (GPU BDF) or "ReactorNull" (forcing only);
+ * "ReactorRK64"/"ReactorArkode" are rejected. mechanism: a mechanism compiled into the library
+ * (pgb_mechanism_info). reactor_type must be 2 (rho h, constant pressure), the value PeleLM uses.
+ * options: whitespace/semicolon separated key=value pairs — the reference's runtime keys
+ * ode.rtol, ode.atol, cvode.max_order, cvode.solve_type, ode.analytical_jacobian,
+ * peleLM.use_typ_vals_chem, plus ode.max_steps, gb.precision=fp64|mixed, gb.tpb, gb.graph=0|1.
+ * Returns NULL on error. */
+pgb_reactor* pgb_reactor_create(const char* name, const char* mechanism, int reactor_type,
+                                const char* options);
+
+/* ReactorBase::set_typ_vals_ode (Source/PeleLM.cpp:1497-1516): n = NUM_SPECIES+1 typical values
+ * (rhoY in CGS, then T). With use_typ_vals_chem=1 the absolute tolerance becomes
+ * ode.atol * typ[i]. */
+int pgb_reactor_set_typ_vals_ode(pgb_reactor* r, const double* typ, int n);
+
+/* ReactorBase::react for one box (Source/PeleLM.cpp:5752): advances every cell of view->box
+ * over *dt_react on `stream` (a cudaStream_t, may be NULL) and waits for it. rY, T, rEner and
+ * FC are updated in place. *dt_react and *time are left unchanged (the caller resets them,
+ * Source/PeleLM.cpp:5759-5760). Returns the number of cells that failed (FC < 0 marks them). */
+int pgb_reactor_react(pgb_reactor* r, const pgb_box_view* view, double* dt_react, double* time,
+                      void* stream);
+
+/* All boxes of all levels in one persistent launch with a work-stealing cell queue. Stream
+ * ordered and asynchronous (returns 0 once enqueued); with gb.graph=1 and a non-default stream
+ * the enqueue is captured once per box set into a CUDA graph and replayed. */
+int pgb_reactor_react_boxes(pgb_reactor* r, const pgb_box_view* views, int nbox, double dt_react,
+                            double time, void* stream);
+
+/* Waits for the last advance on its stream and returns its counters. */
+int pgb_reactor_get_stats(pgb_reactor* r, pgb_stats* out);
+
+/* ReactorBase::close (Source/PeleLM.cpp:930) and destruction. */
+void pgb_reactor_close(pgb_reactor* r);
+
+/* Copies the last error message of the calling thread; returns its length. */
+int pgb_last_error(char* buf, size_t n);
+
+/* Species / reaction counts of a compiled mechanism; returns 0 if known, -1 otherwise. */
+int pgb_mechanism_info(const char* mechanism, int* nspecies, int* nreactions);
+
+/* Library identification (ABI version, build arch). */
+int pgb_version(void);
+
+/* Instantaneous production rates, the per-cell work of reactionRateRhoY
+ * (Source/PeleLM_K.H:54-98) called from compute_instantaneous_reaction_rates
+ * (Source/PeleLM.cpp:2013-2074). MKS in and out, as there: rhoY (kg/m^3), rhoH (J/m^3), T (K,
+ * initial guess, refined by HY2T), mask; writes rhoYdot (kg/m^3/s). The view's rY_src / rEner_src
+ * / FC fields are unused; rhoYdot goes to `out`. */
+int pgb_reaction_rates(const char* mechanism, const pgb_box_view* view, const pgb_array4* out,
+                       void* stream);
+
+/* T from (rho h, Y): the per-cell work of RhoH_to_Temp / getTfromHY (Source/PeleLM.cpp:8201-8287,
+ * Source/PeleLM_K.H:508-529). MKS in: rhoY (view->rY), rhoH (view->rEner), T in/out (view->T).
+ * Newton iteration clipped to [tmin, tmax]. */
+int pgb_rhoh_to_temp(const char* mechanism, const pgb_box_view* view, double tmin, double tmax,
+                     void* stream);
+
+/* Measures the device's FP64 FMA throughput in TFLOP/s (2 flops per FMA). No counterpart in
+ * the reference: a measurement utility giving the roofline denominator of the FP64-bound
+ * reactor kernels. */
+int pgb_fp64_peak_tflops(int iters, double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PELELM_GB300_H */

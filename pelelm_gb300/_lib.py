@@ -1,0 +1,83 @@
+"""ctypes binding of the native library's C ABI (include/pelelm_gb300.h).
+
+The library is the product; this module only declares its entry points. Loading fails
+loudly when the library has not been built — there is no fallback implementation.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from ._build import LIB
+
+_vp = C.c_void_p
+
+
+class Array4(C.Structure):
+    _fields_ = [("p", C.c_void_p), ("jstride", C.c_longlong), ("kstride", C.c_longlong),
+                ("nstride", C.c_longlong), ("begin", C.c_int * 3), ("end", C.c_int * 3),
+                ("ncomp", C.c_int)]
+
+
+class Box(C.Structure):
+    _fields_ = [("lo", C.c_int * 3), ("hi", C.c_int * 3)]
+
+
+class BoxView(C.Structure):
+    _fields_ = [("box", Box), ("rY", Array4), ("rY_src", Array4), ("T", Array4),
+                ("rEner", Array4), ("rEner_src", Array4), ("FC", Array4), ("mask", Array4)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("ncell", C.c_ulonglong), ("nst", C.c_ulonglong), ("nfe", C.c_ulonglong),
+                ("nje", C.c_ulonglong), ("netf", C.c_ulonglong), ("ncfn", C.c_ulonglong),
+                ("nfail", C.c_ulonglong), ("max_nst", C.c_ulonglong), ("hist", C.c_ulonglong * 16)]
+
+
+EXPORTS = {
+    "pgb_version": (C.c_int, []),
+    "pgb_last_error": (C.c_int, [C.c_char_p, C.c_size_t]),
+    "pgb_mechanism_info": (C.c_int, [C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "pgb_reactor_create": (_vp, [C.c_char_p, C.c_char_p, C.c_int, C.c_char_p]),
+    "pgb_reactor_set_typ_vals_ode": (C.c_int, [_vp, C.POINTER(C.c_double), C.c_int]),
+    "pgb_reactor_react": (C.c_int, [_vp, C.POINTER(BoxView), C.POINTER(C.c_double),
+                                    C.POINTER(C.c_double), _vp]),
+    "pgb_reactor_react_boxes": (C.c_int, [_vp, C.POINTER(BoxView), C.c_int, C.c_double,
+                                          C.c_double, _vp]),
+    "pgb_reactor_get_stats": (C.c_int, [_vp, C.POINTER(Stats)]),
+    "pgb_reactor_close": (None, [_vp]),
+    "pgb_reaction_rates": (C.c_int, [C.c_char_p, C.POINTER(BoxView), C.POINTER(Array4), _vp]),
+    "pgb_rhoh_to_temp": (C.c_int, [C.c_char_p, C.POINTER(BoxView), C.c_double, C.c_double, _vp]),
+    "pgb_fp64_peak_tflops": (C.c_int, [C.c_int, C.POINTER(C.c_double)]),
+}
+
+_lib = None
+
+
+def lib():
+    """Load the native library (building it first is the caller's job: __graft_entry__.build
+    or ``python -m pelelm_gb300._build``)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            raise RuntimeError(f"pelelm_gb300 native library missing ({LIB}); build it with "
+                               "`python -m pelelm_gb300._build`")
+        L = C.CDLL(LIB)
+        for name, (res, args) in EXPORTS.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def last_error() -> str:
+    buf = C.create_string_buffer(1024)
+    lib().pgb_last_error(buf, len(buf))
+    return buf.value.decode(errors="replace")
+
+
+def check(rc: int, what: str) -> int:
+    if rc < 0:
+        raise RuntimeError(f"{what} failed: {last_error()}")
+    return rc

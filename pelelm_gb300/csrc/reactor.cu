@@ -1,0 +1,424 @@
+// Host driver and C ABI of the GB300 reactor (include/pelelm_gb300.h).
+//
+// Stands in for the PelePhysics ReactorBase implementations that PeleLM reaches through
+// m_reactor (Source/PeleLM.H:673-674): create/init (Source/PeleLM.cpp:706-709),
+// set_typ_vals_ode (:1513), react (:5752) and close (:930), plus a multi-box entry point that
+// advances every box of every level in one persistent launch.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "reactor_registry.cuh"
+
+namespace pgb_host {
+
+namespace {
+thread_local std::string g_err;
+}
+
+int set_err(const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return -1;
+}
+
+extern const MechEntry kEntry_lidryer_syn;
+extern const MechEntry kEntry_drm19_syn;
+
+}  // namespace pgb_host
+
+using namespace pgb_host;
+
+namespace {
+
+// ------------------------------------------------------------------ options
+struct Options {
+  double rtol = 1e-6;
+  double atol = 1e-10;
+  int max_order = 5;
+  int max_steps = 20000;
+  bool use_typ_vals = false;
+  bool mixed = true;       // gb.precision = mixed (FP32 J/LU) | fp64
+  int tpb = 0;             // 0 = default per mechanism
+  bool graph = false;
+  std::string solve_type = "denseAJ_direct";
+  int analytical_jacobian = 1;
+};
+
+int parse_options(const char* s, Options& o) {
+  if (!s) return 0;
+  std::string str(s);
+  for (char& c : str)
+    if (c == ';' || c == ',' || c == '\n' || c == '\t') c = ' ';
+  std::istringstream is(str);
+  std::string tok;
+  while (is >> tok) {
+    const size_t eq = tok.find('=');
+    if (eq == std::string::npos) return set_err("option '%s' is not key=value", tok.c_str());
+    const std::string k = tok.substr(0, eq), v = tok.substr(eq + 1);
+    try {
+      if (k == "ode.rtol") o.rtol = std::stod(v);
+      else if (k == "ode.atol") o.atol = std::stod(v);
+      else if (k == "cvode.max_order") o.max_order = std::stoi(v);
+      else if (k == "ode.max_steps") o.max_steps = std::stoi(v);
+      else if (k == "peleLM.use_typ_vals_chem") o.use_typ_vals = std::stoi(v) != 0;
+      else if (k == "cvode.solve_type") o.solve_type = v;
+      else if (k == "ode.analytical_jacobian") o.analytical_jacobian = std::stoi(v);
+      else if (k == "gb.precision") {
+        if (v == "mixed") o.mixed = true;
+        else if (v == "fp64") o.mixed = false;
+        else return set_err("gb.precision must be mixed or fp64, got '%s'", v.c_str());
+      } else if (k == "gb.tpb") o.tpb = std::stoi(v);
+      else if (k == "gb.graph") o.graph = std::stoi(v) != 0;
+      else return set_err("unknown option '%s'", k.c_str());
+    } catch (...) {
+      return set_err("bad value for option '%s': '%s'", k.c_str(), v.c_str());
+    }
+  }
+  if (!(o.rtol > 0.0) || !(o.atol > 0.0)) return set_err("ode.rtol and ode.atol must be > 0");
+  if (o.max_order < 1 || o.max_order > pgb::QMAX)
+    return set_err("cvode.max_order must be in [1, %d]", pgb::QMAX);
+  if (o.max_steps < 1) return set_err("ode.max_steps must be >= 1");
+  if (o.solve_type != "denseAJ_direct" && o.solve_type != "dense_direct" && o.solve_type != "dense" &&
+      o.solve_type != "denseFDJ_direct")
+    return set_err("cvode.solve_type '%s' is not provided (dense direct solves only)",
+                   o.solve_type.c_str());
+  return 0;
+}
+
+const MechEntry* find_mech(const char* name);
+
+int build_boxes(const pgb_box_view* v, int nbox, int ns, std::vector<pgb::BoxDev>& out,
+                long long& ncell) {
+  out.resize(nbox);
+  ncell = 0;
+  for (int b = 0; b < nbox; ++b) {
+    const pgb_box& bx = v[b].box;
+    for (int d = 0; d < 3; ++d)
+      if (bx.hi[d] < bx.lo[d]) return set_err("box %d is empty in dim %d", b, d);
+    if (check_arr(v[b].rY, bx, ns, "rY", b) || check_arr(v[b].rY_src, bx, ns, "rY_src", b) ||
+        check_arr(v[b].T, bx, 1, "T", b) || check_arr(v[b].rEner, bx, 1, "rEner", b) ||
+        check_arr(v[b].rEner_src, bx, 1, "rEner_src", b) || check_arr(v[b].FC, bx, 1, "FC", b))
+      return -1;
+    if (v[b].mask.p && check_arr(v[b].mask, bx, 1, "mask", b)) return -1;
+    pgb::BoxDev& d = out[b];
+    d.lo0 = bx.lo[0]; d.lo1 = bx.lo[1]; d.lo2 = bx.lo[2];
+    d.len0 = bx.hi[0] - bx.lo[0] + 1;
+    d.len1 = bx.hi[1] - bx.lo[1] + 1;
+    d.len2 = bx.hi[2] - bx.lo[2] + 1;
+    d.cell_offset = ncell;
+    ncell += (long long)d.len0 * d.len1 * d.len2;
+    d.rY = arr_dev(v[b].rY);
+    d.rYsrc = arr_dev(v[b].rY_src);
+    d.T = arr_dev(v[b].T);
+    d.rE = arr_dev(v[b].rEner);
+    d.rEsrc = arr_dev(v[b].rEner_src);
+    d.FC = arr_dev(v[b].FC);
+    d.mask.p = static_cast<const int*>(v[b].mask.p);
+    d.mask.jstride = v[b].mask.jstride;
+    d.mask.kstride = v[b].mask.kstride;
+    d.mask.begin0 = v[b].mask.begin[0];
+    d.mask.begin1 = v[b].mask.begin[1];
+    d.mask.begin2 = v[b].mask.begin[2];
+  }
+  return 0;
+}
+
+// ------------------------------------------------------------------ per-stream scratch
+struct Scratch {
+  pgb::BoxDev* d_boxes = nullptr;
+  size_t box_cap = 0;
+  pgb::BoxDev* h_boxes = nullptr;  // pinned staging
+  unsigned long long* d_counter = nullptr;
+  pgb::ReactStats* d_stats = nullptr;
+  cudaEvent_t done = nullptr;
+  long long last_ncell = 0;
+  // graph cache
+  cudaGraphExec_t gexec = nullptr;
+  std::vector<pgb::BoxDev> gkey;
+  double gdt = -1.0;
+};
+
+}  // namespace
+
+struct pgb_reactor {
+  std::string name;
+  const MechEntry* mech = nullptr;
+  Options opt;
+  bool null_reactor = false;
+  std::vector<double> typ;
+  std::mutex mu;
+  std::map<cudaStream_t, Scratch> scratch;
+  cudaStream_t last_stream = nullptr;
+  int device = 0, nsm = 0;
+};
+
+namespace {
+
+void free_scratch(Scratch& s) {
+  if (s.gexec) cudaGraphExecDestroy(s.gexec);
+  if (s.d_boxes) cudaFree(s.d_boxes);
+  if (s.h_boxes) cudaFreeHost(s.h_boxes);
+  if (s.d_counter) cudaFree(s.d_counter);
+  if (s.d_stats) cudaFree(s.d_stats);
+  if (s.done) cudaEventDestroy(s.done);
+  s = Scratch();
+}
+
+int ensure_scratch(pgb_reactor* r, cudaStream_t st, size_t nbox, Scratch** out) {
+  Scratch& s = r->scratch[st];
+  if (!s.d_counter) {
+    PGB_CUDA(cudaMalloc(&s.d_counter, sizeof(unsigned long long)));
+    PGB_CUDA(cudaMalloc(&s.d_stats, sizeof(pgb::ReactStats)));
+    PGB_CUDA(cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming));
+  }
+  if (nbox > s.box_cap) {
+    if (s.done) PGB_CUDA(cudaEventSynchronize(s.done));
+    if (s.gexec) { cudaGraphExecDestroy(s.gexec); s.gexec = nullptr; s.gkey.clear(); }
+    if (s.d_boxes) PGB_CUDA(cudaFree(s.d_boxes));
+    if (s.h_boxes) PGB_CUDA(cudaFreeHost(s.h_boxes));
+    size_t cap = std::max<size_t>(nbox, 64);
+    PGB_CUDA(cudaMalloc(&s.d_boxes, cap * sizeof(pgb::BoxDev)));
+    PGB_CUDA(cudaMallocHost(&s.h_boxes, cap * sizeof(pgb::BoxDev)));
+    s.box_cap = cap;
+  }
+  *out = &s;
+  return 0;
+}
+
+bool same_boxes(const std::vector<pgb::BoxDev>& a, const pgb::BoxDev* b, size_t n) {
+  return a.size() == n && std::memcmp(a.data(), b, n * sizeof(pgb::BoxDev)) == 0;
+}
+
+int default_tpb(const pgb_reactor* r) {
+  const int per = r->opt.mixed ? r->mech->smem_mixed : r->mech->smem_fp64;
+  const int limit = 227 * 1024;
+  if (per * 128 <= limit) return 128;
+  return 64;
+}
+
+int enqueue_advance(pgb_reactor* r, Scratch& s, int nbox, long long ncell, double dt,
+                    cudaStream_t st) {
+  pgb::ReactParams p;
+  std::memset(&p, 0, sizeof(p));
+  p.boxes = s.d_boxes;
+  p.nbox = nbox;
+  p.ncell = ncell;
+  p.dt = dt;
+  p.rtol = r->opt.rtol;
+  const int N = r->mech->ns + 1;
+  for (int i = 0; i < N; ++i)
+    p.atol[i] = (r->opt.use_typ_vals && (int)r->typ.size() == N) ? r->opt.atol * r->typ[i] : r->opt.atol;
+  p.max_order = r->opt.max_order;
+  p.max_steps = r->opt.max_steps;
+  p.next_cell = s.d_counter;
+  p.stats = s.d_stats;
+  PGB_CUDA(cudaMemcpyAsync(s.d_boxes, s.h_boxes, nbox * sizeof(pgb::BoxDev), cudaMemcpyHostToDevice, st));
+  PGB_CUDA(cudaMemsetAsync(s.d_counter, 0, sizeof(unsigned long long), st));
+  PGB_CUDA(cudaMemsetAsync(s.d_stats, 0, sizeof(pgb::ReactStats), st));
+  if (ncell == 0) return 0;
+  if (r->null_reactor) {
+    const long long nb = std::min<long long>((ncell + 255) / 256, (long long)r->nsm * 8);
+    return r->mech->null_fn(p, st, (int)nb);
+  }
+  const int tpb = r->opt.tpb > 0 ? r->opt.tpb : default_tpb(r);
+  // persistent grid: one CTA per SM (the shared-memory footprint admits one), never more
+  // CTAs than there are warps' worth of cells
+  const long long max_blocks = std::max<long long>(1, (ncell + tpb - 1) / tpb);
+  const int nblocks = (int)std::min<long long>(r->nsm, max_blocks);
+  LaunchFn fn = r->opt.mixed ? r->mech->bdf_mixed : r->mech->bdf_fp64;
+  return fn(p, tpb, st, nblocks);
+}
+
+}  // namespace
+
+// ================================================================== C ABI
+extern "C" {
+
+int pgb_version(void) { return PGB_ABI_VERSION; }
+
+int pgb_last_error(char* buf, size_t n) {
+  if (buf && n) {
+    std::strncpy(buf, g_err.c_str(), n - 1);
+    buf[n - 1] = 0;
+  }
+  return (int)g_err.size();
+}
+
+int pgb_mechanism_info(const char* mechanism, int* ns, int* nr) {
+  const MechEntry* m = find_mech(mechanism);
+  if (!m) return set_err("unknown mechanism '%s'", mechanism ? mechanism : "(null)");
+  if (ns) *ns = m->ns;
+  if (nr) *nr = m->nr;
+  return 0;
+}
+
+pgb_reactor* pgb_reactor_create(const char* name, const char* mechanism, int reactor_type,
+                                const char* options) {
+  std::string n = name ? name : "";
+  if (n == "ReactorRK64" || n == "ReactorArkode") {
+    set_err("reactor '%s' is not provided by this library (ReactorCvode, ReactorNull)", n.c_str());
+    return nullptr;
+  }
+  if (n != "ReactorCvode" && n != "ReactorNull") {
+    set_err("unknown reactor '%s'", n.c_str());
+    return nullptr;
+  }
+  if (reactor_type != 2) {
+    set_err("reactor_type %d not supported: only 2 (rho h, constant pressure) as PeleLM uses",
+            reactor_type);
+    return nullptr;
+  }
+  const MechEntry* m = find_mech(mechanism);
+  if (!m) {
+    set_err("unknown mechanism '%s'", mechanism ? mechanism : "(null)");
+    return nullptr;
+  }
+  Options o;
+  if (parse_options(options, o)) return nullptr;
+  int dev = 0, nsm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+    set_err("no CUDA device available");
+    return nullptr;
+  }
+  auto* r = new pgb_reactor();
+  r->name = n;
+  r->mech = m;
+  r->opt = o;
+  r->null_reactor = (n == "ReactorNull");
+  r->device = dev;
+  r->nsm = nsm;
+  return r;
+}
+
+int pgb_reactor_set_typ_vals_ode(pgb_reactor* r, const double* typ, int n) {
+  if (!r) return set_err("null reactor");
+  if (n != r->mech->ns + 1) return set_err("set_typ_vals_ode: expected %d values, got %d", r->mech->ns + 1, n);
+  std::lock_guard<std::mutex> g(r->mu);
+  r->typ.assign(typ, typ + n);
+  for (auto& kv : r->scratch)  // tolerances are baked into captured graphs
+    if (kv.second.gexec) { cudaGraphExecDestroy(kv.second.gexec); kv.second.gexec = nullptr; kv.second.gkey.clear(); }
+  return 0;
+}
+
+int pgb_reactor_react_boxes(pgb_reactor* r, const pgb_box_view* views, int nbox, double dt_react,
+                            double time, void* stream) {
+  (void)time;
+  if (!r) return set_err("null reactor");
+  if (nbox < 0 || (nbox > 0 && !views)) return set_err("bad box list");
+  if (!(dt_react > 0.0)) return set_err("dt_react must be > 0");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  std::lock_guard<std::mutex> g(r->mu);
+  Scratch* s = nullptr;
+  if (ensure_scratch(r, st, std::max(nbox, 1), &s)) return -1;
+  std::vector<pgb::BoxDev> boxes;
+  long long ncell = 0;
+  if (build_boxes(views, nbox, r->mech->ns, boxes, ncell)) return -1;
+  PGB_CUDA(cudaEventSynchronize(s->done));  // staging buffer may still feed a previous copy
+  if (nbox) std::memcpy(s->h_boxes, boxes.data(), nbox * sizeof(pgb::BoxDev));
+  s->last_ncell = ncell;
+  r->last_stream = st;
+  if (r->opt.graph && st != nullptr) {
+    if (!(s->gexec && s->gdt == dt_react && same_boxes(s->gkey, boxes.data(), nbox))) {
+      if (s->gexec) { cudaGraphExecDestroy(s->gexec); s->gexec = nullptr; }
+      cudaGraph_t graph;
+      PGB_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+      const int rc = enqueue_advance(r, *s, nbox, ncell, dt_react, st);
+      const cudaError_t ec = cudaStreamEndCapture(st, &graph);
+      if (rc) return rc;
+      if (ec != cudaSuccess) return set_err("graph capture failed: %s", cudaGetErrorString(ec));
+      PGB_CUDA(cudaGraphInstantiate(&s->gexec, graph, 0));
+      cudaGraphDestroy(graph);
+      s->gkey = boxes;
+      s->gdt = dt_react;
+    }
+    PGB_CUDA(cudaGraphLaunch(s->gexec, st));
+  } else {
+    if (enqueue_advance(r, *s, nbox, ncell, dt_react, st)) return -1;
+  }
+  PGB_CUDA(cudaEventRecord(s->done, st));
+  return 0;
+}
+
+int pgb_reactor_get_stats(pgb_reactor* r, pgb_stats* out) {
+  if (!r || !out) return set_err("null argument");
+  std::lock_guard<std::mutex> g(r->mu);
+  auto it = r->scratch.find(r->last_stream);
+  if (it == r->scratch.end()) return set_err("no advance has run yet");
+  Scratch& s = it->second;
+  pgb::ReactStats h;
+  PGB_CUDA(cudaEventSynchronize(s.done));
+  PGB_CUDA(cudaMemcpy(&h, s.d_stats, sizeof(h), cudaMemcpyDeviceToHost));
+  out->ncell = (unsigned long long)s.last_ncell;
+  out->nst = h.nst; out->nfe = h.nfe; out->nje = h.nje; out->netf = h.netf; out->ncfn = h.ncfn;
+  out->nfail = h.nfail; out->max_nst = h.max_nst;
+  for (int i = 0; i < 16; ++i) out->hist[i] = h.hist[i];
+  return 0;
+}
+
+int pgb_reactor_react(pgb_reactor* r, const pgb_box_view* view, double* dt_react, double* time,
+                      void* stream) {
+  if (!r || !view || !dt_react || !time) return set_err("null argument");
+  if (pgb_reactor_react_boxes(r, view, 1, *dt_react, *time, stream)) return -1;
+  pgb_stats st;
+  if (pgb_reactor_get_stats(r, &st)) return -1;
+  return (int)st.nfail;
+}
+
+void pgb_reactor_close(pgb_reactor* r) {
+  if (!r) return;
+  {
+    std::lock_guard<std::mutex> g(r->mu);
+    for (auto& kv : r->scratch) {
+      if (kv.second.done) cudaEventSynchronize(kv.second.done);
+      free_scratch(kv.second);
+    }
+  }
+  delete r;
+}
+
+int pgb_reaction_rates(const char* mechanism, const pgb_box_view* view, const pgb_array4* out,
+                       void* stream) {
+  const MechEntry* m = find_mech(mechanism);
+  if (!m) return set_err("unknown mechanism '%s'", mechanism ? mechanism : "(null)");
+  if (!view || !out) return set_err("null argument");
+  return m->rates_fn(view, out, static_cast<cudaStream_t>(stream));
+}
+
+int pgb_rhoh_to_temp(const char* mechanism, const pgb_box_view* view, double tmin, double tmax,
+                     void* stream) {
+  const MechEntry* m = find_mech(mechanism);
+  if (!m) return set_err("unknown mechanism '%s'", mechanism ? mechanism : "(null)");
+  if (!view) return set_err("null argument");
+  if (!(tmin > 0.0 && tmax > tmin)) return set_err("need 0 < tmin < tmax");
+  return m->h2t_fn(view, tmin, tmax, static_cast<cudaStream_t>(stream));
+}
+
+}  // extern "C"
+
+namespace {
+
+const MechEntry* const kMechs[] = {&kEntry_lidryer_syn, &kEntry_drm19_syn};
+
+const MechEntry* find_mech(const char* name) {
+  if (!name) return nullptr;
+  for (const MechEntry* m : kMechs)
+    if (std::strcmp(m->name, name) == 0) return m;
+  return nullptr;
+}
+
+}  // namespace

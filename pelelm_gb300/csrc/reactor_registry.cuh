@@ -1,0 +1,143 @@
+// Mechanism registry shared by the per-mechanism translation units and the host driver.
+// Each mech_<name>.cu instantiates the kernels of one mechanism and exports one MechEntry.
+#ifndef PGB_REACTOR_REGISTRY_CUH
+#define PGB_REACTOR_REGISTRY_CUH
+
+#include <cuda_runtime.h>
+
+#include "../../include/pelelm_gb300.h"
+#include "bdf_kernel.cuh"
+#include "point_kernels.cuh"
+#include "reactor_types.cuh"
+
+namespace pgb_host {
+
+// Records the calling thread's error message (pgb_last_error) and returns -1.
+int set_err(const char* fmt, ...);
+
+#define PGB_CUDA(call)                                                                       \
+  do {                                                                                       \
+    cudaError_t e_ = (call);                                                                 \
+    if (e_ != cudaSuccess) return ::pgb_host::set_err("%s: %s (%s:%d)", #call,              \
+                                                      cudaGetErrorString(e_), __FILE__, __LINE__); \
+  } while (0)
+
+using LaunchFn = int (*)(const pgb::ReactParams&, int tpb, cudaStream_t, int nblocks);
+
+constexpr int kMaxSmemPerBlock = 227 * 1024;
+
+template <class M, class JR, int TPB>
+int launch_bdf_tpb(const pgb::ReactParams& p, cudaStream_t s, int nblocks) {
+  constexpr int smem = pgb::bdf_smem_per_thread<M, JR>() * TPB;
+  if constexpr (smem > kMaxSmemPerBlock) {
+    return set_err("%s: %d threads per block need %d B of shared memory (limit %d)", M::NAME, TPB,
+                   smem, kMaxSmemPerBlock);
+  } else {
+    auto kern = pgb::bdf_reactor_kernel<M, JR, TPB>;
+    PGB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    kern<<<nblocks, TPB, smem, s>>>(p);
+    PGB_CUDA(cudaGetLastError());
+    return 0;
+  }
+}
+
+template <class M, class JR>
+int launch_bdf(const pgb::ReactParams& p, int tpb, cudaStream_t s, int nblocks) {
+  switch (tpb) {
+    case 64: return launch_bdf_tpb<M, JR, 64>(p, s, nblocks);
+    case 128: return launch_bdf_tpb<M, JR, 128>(p, s, nblocks);
+    default: return set_err("gb.tpb=%d is not compiled (64, 128)", tpb);
+  }
+}
+
+template <class M>
+int launch_null(const pgb::ReactParams& p, cudaStream_t s, int nblocks) {
+  pgb::null_reactor_kernel<M><<<nblocks, 256, 0, s>>>(p);
+  PGB_CUDA(cudaGetLastError());
+  return 0;
+}
+
+struct MechEntry {
+  const char* name;
+  int ns, nr;
+  LaunchFn bdf_mixed, bdf_fp64;
+  int (*null_fn)(const pgb::ReactParams&, cudaStream_t, int);
+  int smem_mixed, smem_fp64;  // bytes per thread
+  int (*rates_fn)(const pgb_box_view*, const pgb_array4*, cudaStream_t);
+  int (*h2t_fn)(const pgb_box_view*, double, double, cudaStream_t);
+};
+
+
+
+inline pgb::ArrDev arr_dev(const pgb_array4& a) {
+  pgb::ArrDev d;
+  d.p = static_cast<double*>(a.p);
+  d.jstride = a.jstride;
+  d.kstride = a.kstride;
+  d.nstride = a.nstride;
+  d.begin0 = a.begin[0];
+  d.begin1 = a.begin[1];
+  d.begin2 = a.begin[2];
+  return d;
+}
+
+inline int check_arr(const pgb_array4& a, const pgb_box& b, int ncomp, const char* what, int ibox) {
+  if (!a.p) return set_err("box %d: array %s is NULL", ibox, what);
+  for (int d = 0; d < 3; ++d)
+    if (b.lo[d] < a.begin[d] || b.hi[d] >= a.end[d])
+      return set_err("box %d: array %s [%d,%d) in dim %d does not cover the box [%d,%d]", ibox,
+                     what, a.begin[d], a.end[d], d, b.lo[d], b.hi[d]);
+  if (a.ncomp < ncomp) return set_err("box %d: array %s has %d comps, need %d", ibox, what, a.ncomp, ncomp);
+  return 0;
+}
+
+template <class M>
+int rates_entry(const pgb_box_view* v, const pgb_array4* out, cudaStream_t s) {
+  const pgb_box& b = v->box;
+  if (check_arr(v->rY, b, M::NS, "rY", 0) || check_arr(v->T, b, 1, "T", 0) ||
+      check_arr(v->rEner, b, 1, "rEner", 0) || check_arr(*out, b, M::NS, "out", 0))
+    return -1;
+  if (v->mask.p && check_arr(v->mask, b, 1, "mask", 0)) return -1;
+  pgb::PointParams p;
+  p.lo0 = b.lo[0]; p.lo1 = b.lo[1]; p.lo2 = b.lo[2];
+  p.len0 = b.hi[0] - b.lo[0] + 1; p.len1 = b.hi[1] - b.lo[1] + 1; p.len2 = b.hi[2] - b.lo[2] + 1;
+  p.rY = arr_dev(v->rY); p.rE = arr_dev(v->rEner); p.T = arr_dev(v->T); p.out = arr_dev(*out);
+  p.mask.p = static_cast<const int*>(v->mask.p);
+  p.mask.jstride = v->mask.jstride; p.mask.kstride = v->mask.kstride;
+  p.mask.begin0 = v->mask.begin[0]; p.mask.begin1 = v->mask.begin[1]; p.mask.begin2 = v->mask.begin[2];
+  const long long n = (long long)p.len0 * p.len1 * p.len2;
+  if (n == 0) return 0;
+  pgb::rates_kernel<M><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(p);
+  PGB_CUDA(cudaGetLastError());
+  return 0;
+}
+
+template <class M>
+int h2t_entry(const pgb_box_view* v, double tmin, double tmax, cudaStream_t s) {
+  const pgb_box& b = v->box;
+  if (check_arr(v->rY, b, M::NS, "rY", 0) || check_arr(v->T, b, 1, "T", 0) ||
+      check_arr(v->rEner, b, 1, "rEner", 0))
+    return -1;
+  pgb::PointParams p;
+  p.lo0 = b.lo[0]; p.lo1 = b.lo[1]; p.lo2 = b.lo[2];
+  p.len0 = b.hi[0] - b.lo[0] + 1; p.len1 = b.hi[1] - b.lo[1] + 1; p.len2 = b.hi[2] - b.lo[2] + 1;
+  p.rY = arr_dev(v->rY); p.rE = arr_dev(v->rEner); p.T = arr_dev(v->T);
+  p.tmin = tmin; p.tmax = tmax;
+  const long long n = (long long)p.len0 * p.len1 * p.len2;
+  if (n == 0) return 0;
+  pgb::h2t_kernel<M><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(p);
+  PGB_CUDA(cudaGetLastError());
+  return 0;
+}
+
+#define PGB_MECH_ENTRY(M)                                                                    \
+  ::pgb_host::MechEntry {                                                                    \
+    M::NAME, M::NS, M::NR, ::pgb_host::launch_bdf<M, float>, ::pgb_host::launch_bdf<M, double>, \
+        ::pgb_host::launch_null<M>, pgb::bdf_smem_per_thread<M, float>(),                    \
+        pgb::bdf_smem_per_thread<M, double>(), ::pgb_host::rates_entry<M>,                   \
+        ::pgb_host::h2t_entry<M>                                                             \
+  }
+
+}  // namespace pgb_host
+
+#endif  // PGB_REACTOR_REGISTRY_CUH

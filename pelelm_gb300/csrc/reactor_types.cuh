@@ -1,0 +1,58 @@
+// Device-side descriptors shared by the reactor kernels and the host driver.
+#ifndef PGB_REACTOR_TYPES_CUH
+#define PGB_REACTOR_TYPES_CUH
+
+#include <stdint.h>
+
+namespace pgb {
+
+constexpr int QMAX = 5;     // highest BDF order supported (cvode.max_order <= 5)
+constexpr int MAXN = 64;    // largest ODE size (species + 1) any built mechanism uses
+
+// One Array4-like view: element (i,j,k,n) lives at
+// p[(i-begin0) + (j-begin1)*jstride + (k-begin2)*kstride + n*nstride].
+struct ArrDev {
+  double* p;
+  long long jstride, kstride, nstride;
+  int begin0, begin1, begin2;
+};
+
+struct MaskDev {
+  const int* p;
+  long long jstride, kstride;
+  int begin0, begin1, begin2;
+};
+
+// One box of cells; cells are numbered i fastest, then j, then k, starting at
+// cell_offset within the flat cell index space of one launch.
+struct BoxDev {
+  int lo0, lo1, lo2;
+  int len0, len1, len2;
+  long long cell_offset;
+  ArrDev rY, rYsrc, T, rE, rEsrc, FC;
+  MaskDev mask;  // p may be null: all cells active
+};
+
+// Per-launch counters (device scratch, zeroed before each launch).
+struct ReactStats {
+  unsigned long long nst, nfe, nje, netf, ncfn, nfail;
+  unsigned long long max_nst;
+  unsigned long long hist[16];  // steps per cell, bins [2^b, 2^(b+1))
+};
+
+struct ReactParams {
+  const BoxDev* boxes;
+  int nbox;
+  long long ncell;
+  double dt;
+  double rtol;
+  double atol[MAXN];
+  int max_order;
+  int max_steps;
+  unsigned long long* next_cell;  // work queue head (device scratch)
+  ReactStats* stats;              // device scratch
+};
+
+}  // namespace pgb
+
+#endif  // PGB_REACTOR_TYPES_CUH

@@ -1,0 +1,447 @@
+"""CUDA code generator for a mechanism: one header per mechanism with fully unrolled
+production rates, reactor right-hand side and analytic Jacobian.
+
+Plays the role FUEGO plays for PelePhysics (``Docs/source/manual/Model.rst:296-310``:
+mechanism-specific generated rate/thermo code), written from scratch for sm_103a:
+
+* all mechanism constants are folded into immediates (ln A, Ea/R, 1/W, NASA-7 with the
+  per-species coefficient set picked by a predicated select, never a divergent branch);
+* rates evaluate ln k in FP64 FMAs and take one exponential per coefficient;
+* the Jacobian is a template on its arithmetic type: ``float`` recomputes every rate
+  coefficient in FP32 (the inexact-Newton preconditioner), ``double`` gives the plain
+  FP64 Jacobian. It writes J(i,k) through an accessor so the caller decides where the
+  matrix lives (shared memory per thread).
+
+The formulas are those of the CPU oracle (``oracle/chem_oracle.cpp``), which is the
+equation-level restatement of Model.rst:227-296.
+"""
+from __future__ import annotations
+
+import math
+import os
+from typing import Dict, List
+
+from .model import Mechanism, R_CAL, R_ERG, P_ATM
+
+LN10 = math.log(10.0)
+
+
+def _f(x: float) -> str:
+    r = repr(float(x))
+    if "e" not in r and "." not in r and "inf" not in r and "nan" not in r:
+        r += ".0"
+    return r
+
+
+class _Emitter:
+    def __init__(self):
+        self.lines: List[str] = []
+        self.ind = 0
+
+    def __call__(self, s: str = ""):
+        self.lines.append("  " * self.ind + s if s else "")
+
+    def text(self) -> str:
+        return "\n".join(self.lines) + "\n"
+
+
+def _thermo_select(e: _Emitter, m: Mechanism, prec: str):
+    """Emit per-species NASA-7 coefficient selects a{k}_{i} for the current T."""
+    tmids = sorted({s.Tmid for s in m.species})
+    for t in tmids:
+        e(f"const bool lo_{int(t)} = T < {_f(t)};")
+    cast = "" if prec == "double" else "f"
+    for k, s in enumerate(m.species):
+        for i in range(7):
+            lo, hi = s.low[i], s.high[i]
+            e(f"const {prec} a{k}_{i} = lo_{int(s.Tmid)} ? {_f(lo)}{cast} : {_f(hi)}{cast};")
+
+
+def _sel(lo_flag: str, lo: float, hi: float, prec: str = "double") -> str:
+    """Predicated select between two folded immediates (no branch)."""
+    if prec == "double":
+        return f"({lo_flag} ? {_f(lo)} : {_f(hi)})"
+    return f"({lo_flag} ? R({_f(lo)}) : R({_f(hi)}))"
+
+
+def _g_expr(k, s, lo_flag):
+    """g/RT = a0 (1-lnT) - a1 T/2 - a2 T^2/6 - a3 T^3/12 - a4 T^4/20 + a5/T - a6 (FP64, 6 FMA)."""
+    L, H = s.low, s.high
+    c = lambda i, f: _sel(lo_flag, L[i] * f, H[i] * f)
+    return (f"fma({c(0, 1.0)}, lnT1, fma(T, fma(T, fma(T, fma(T, {c(4, -0.05)}, {c(3, -1.0 / 12.0)}), "
+            f"{c(2, -1.0 / 6.0)}), {c(1, -0.5)}), fma({c(5, 1.0)}, invT, {c(6, -1.0)})))")
+
+
+def _hW_expr(s, lo_flag, scale):
+    """scale * h/RT (FP64, 5 FMA)."""
+    L, H = s.low, s.high
+    c = lambda i, f: _sel(lo_flag, L[i] * f * scale, H[i] * f * scale)
+    return (f"fma(T, fma(T, fma(T, fma(T, {c(4, 0.2)}, {c(3, 0.25)}), {c(2, 1.0 / 3.0)}), {c(1, 0.5)}), "
+            f"fma({c(5, 1.0)}, invT, {c(0, 1.0)}))")
+
+
+def _cpW_expr(s, lo_flag, scale):
+    """scale * cp/R (FP64, 4 FMA)."""
+    L, H = s.low, s.high
+    c = lambda i: _sel(lo_flag, L[i] * scale, H[i] * scale)
+    return f"fma(T, fma(T, fma(T, fma(T, {c(4)}, {c(3)}), {c(2)}), {c(1)}), {c(0)})"
+
+
+def gen_header(m: Mechanism) -> str:
+    ns, nr = m.ns, m.nr
+    N = ns + 1
+    W = [s.W for s in m.species]
+    idx = {s.name: i for i, s in enumerate(m.species)}
+    lnP0_R = math.log(P_ATM / R_ERG)  # ln(P0/R); ln(P0/RT) = lnP0_R - lnT
+    e = _Emitter()
+    guard = f"PGB_MECH_{m.name.upper()}_CUH"
+    e("// GENERATED by pelelm_gb300/mech/codegen.py from pelelm_gb300/data/" + m.name + ".json.")
+    e("// Do not edit. " + ("SYNTHETIC structure-matched mechanism." if m.synthetic else ""))
+    e(f"#ifndef {guard}")
+    e(f"#define {guard}")
+    e('#include "../mech_common.cuh"')
+    e()
+    e("namespace pgb {")
+    e(f"struct Mech_{m.name} {{")
+    e.ind += 1
+    e(f"static constexpr int NS = {ns};")
+    e(f"static constexpr int NR = {nr};")
+    e(f"static constexpr int N = {N};")
+    e(f'static constexpr const char* NAME = "{m.name}";')
+    e(f"static constexpr bool SYNTHETIC = {'true' if m.synthetic else 'false'};")
+    e()
+    # ---------------------------------------------------------------- molecular weights
+    e("__host__ __device__ static constexpr double W(int k) {")
+    e("  return " + " ".join(f"k == {k} ? {_f(w)} :" for k, w in enumerate(W)) + " 0.0;")
+    e("}")
+    e()
+    # ---------------------------------------------------------------- thermo (mixture h, cp)
+    e("// Mixture mass enthalpy [erg/g] and cp [erg/g/K] at T for mass fractions Y.")
+    e("__device__ __forceinline__ static void h_cp_mix(const double T, const double* __restrict__ Y, double& h, double& cp) {")
+    e.ind += 1
+    e("const double invT = 1.0 / T;")
+    for t in sorted({s.Tmid for s in m.species}):
+        e(f"const bool lo_{int(t)} = T < {_f(t)};")
+    e("double hs = 0.0, cps = 0.0;")
+    for k, sp in enumerate(m.species):
+        lf = f"lo_{int(sp.Tmid)}"
+        e(f"hs = fma(Y[{k}], {_hW_expr(sp, lf, 1.0 / W[k])}, hs);")
+        e(f"cps = fma(Y[{k}], {_cpW_expr(sp, lf, 1.0 / W[k])}, cps);")
+    e(f"h = hs * ({_f(R_ERG)} * T);")
+    e(f"cp = cps * {_f(R_ERG)};")
+    e.ind -= 1
+    e("}")
+    e()
+    # ---------------------------------------------------------------- FP64 rates core
+    def emit_rates_fp64(with_energy: bool):
+        """Emit body computing q{j} from T, lnT, invT, C{k}, g{k} (FP64)."""
+        # third-body concentrations
+        needM = any(r.kind != "elementary" for r in m.reactions)
+        if needM:
+            e("const double Ctot = " + " + ".join(f"C{k}" for k in range(ns)) + ";")
+        e(f"const double lnP0RT = {_f(lnP0_R)} - lnT;")
+        for j, r in enumerate(m.reactions):
+            e(f"// R{j}: {r.equation()}")
+            lnA = math.log(r.rate.A)
+            ear = r.rate.Ea / R_CAL
+            e(f"double q{j};")
+            e("{")
+            e.ind += 1
+            e(f"const double lnkf = fma({_f(r.rate.beta)}, lnT, fma({_f(-ear)}, invT, {_f(lnA)}));")
+            if r.kind != "elementary":
+                terms = "Ctot"
+                for sname, eff in r.efficiencies.items():
+                    if eff != 1.0:
+                        terms = f"fma({_f(eff - 1.0)}, C{idx[sname]}, {terms})"
+                e(f"const double M = {terms};")
+            if r.kind == "falloff":
+                lnA0 = math.log(r.low.A)
+                ear0 = r.low.Ea / R_CAL
+                e(f"const double lnk0 = fma({_f(r.low.beta)}, lnT, fma({_f(-ear0)}, invT, {_f(lnA0)}));")
+                # Pr = k0 M / kinf
+                e("const double Pr = M * pgb_exp(lnk0 - lnkf);")
+                if r.troe:
+                    a, T3, T1 = r.troe[:3]
+                    fc = f"fma({_f(1.0 - a)}, pgb_exp(T * {_f(-1.0 / T3)}), {_f(a)} * pgb_exp(T * {_f(-1.0 / T1)}))"
+                    if len(r.troe) > 3:
+                        fc = f"{fc} + pgb_exp(invT * {_f(-r.troe[3])})"
+                    e(f"const double Fcent = {fc};")
+                    e(f"const double lFc = pgb_log(Fcent) * {_f(1.0 / LN10)};")
+                    e("const double cc = fma(-0.67, lFc, -0.4), nn = fma(-1.27, lFc, 0.75);")
+                    e(f"const double lPr = pgb_log(fmax(Pr, 1e-300)) * {_f(1.0 / LN10)} + cc;")
+                    e("const double f1 = lPr / fma(-0.14, lPr, nn);")
+                    e(f"const double Fb = pgb_exp({_f(LN10)} * lFc / fma(f1, f1, 1.0));")
+                    e("const double blend = Pr / (1.0 + Pr) * Fb;")
+                else:
+                    e("const double blend = Pr / (1.0 + Pr);")
+                e("const double kf = pgb_exp(lnkf) * blend;")
+            else:
+                e("const double kf = pgb_exp(lnkf);")
+            pf = " * ".join(f"C{idx[s]}" for s, nu in r.reactants.items() for _ in range(nu))
+            pr = " * ".join(f"C{idx[s]}" for s, nu in r.products.items() for _ in range(nu))
+            if r.reversible:
+                dg = []
+                for s, nu in r.products.items():
+                    dg.append(("+" if nu == 1 else f"+ {nu}.0 *") + f" g{idx[s]}")
+                for s, nu in r.reactants.items():
+                    dg.append(("-" if nu == 1 else f"- {nu}.0 *") + f" g{idx[s]}")
+                dnu = sum(r.products.values()) - sum(r.reactants.values())
+                dgs = " ".join(dg).lstrip("+ ").strip()
+                if dnu != 0:
+                    dgs += f" - {_f(dnu)} * lnP0RT"
+                e(f"const double kr = kf * pgb_exp({dgs});")
+                e(f"q{j} = fma(kf, {pf}, -kr * {pr});")
+            else:
+                e(f"q{j} = kf * {pf};")
+            if r.kind == "three_body":
+                e(f"q{j} *= M;")
+            e.ind -= 1
+            e("}")
+        # production rates
+        for k in range(ns):
+            terms = []
+            for j, r in enumerate(m.reactions):
+                nu = r.products.get(m.species[k].name, 0) - r.reactants.get(m.species[k].name, 0)
+                if nu != 0:
+                    terms.append((nu, j))
+            if not terms:
+                e(f"const double wd{k} = 0.0;")
+                continue
+            expr = ""
+            for nu, j in terms:
+                if expr == "":
+                    expr = (f"q{j}" if nu == 1 else (f"-q{j}" if nu == -1 else f"{_f(nu)} * q{j}"))
+                else:
+                    expr = (f"{expr} + q{j}" if nu == 1 else
+                            (f"{expr} - q{j}" if nu == -1 else f"fma({_f(nu)}, q{j}, {expr})"))
+            e(f"const double wd{k} = {expr};")
+
+    def emit_gibbs():
+        for t in sorted({s.Tmid for s in m.species}):
+            e(f"const bool lo_{int(t)} = T < {_f(t)};")
+        e("const double lnT1 = 1.0 - lnT;")
+        for k, sp in enumerate(m.species):
+            e(f"const double g{k} = {_g_expr(k, sp, f'lo_{int(sp.Tmid)}')};")
+
+    e("// Molar production rates [mol/cm^3/s] from T and concentrations C [mol/cm^3].")
+    e("__device__ __forceinline__ static void wdot(const double T, const double* __restrict__ C_, double* __restrict__ wdot_) {")
+    e.ind += 1
+    e("const double invT = 1.0 / T;")
+    e("const double lnT = pgb_log(T);")
+    for k in range(ns):
+        e(f"const double C{k} = C_[{k}];")
+    emit_gibbs()
+    emit_rates_fp64(False)
+    for k in range(ns):
+        e(f"wdot_[{k}] = wd{k};")
+    e.ind -= 1
+    e("}")
+    e()
+    e("// Reactor RHS (constant-pressure RhoH): y = [rhoY_k (g/cm^3), T], F = rhoY forcing,")
+    e("// Fh = rho h forcing. ydot_k = W_k wdot_k + F_k; dT/dt = (Fh - sum h_k ydot_k) / (rho cp).")
+    e("__device__ __forceinline__ static void rhs(const double* __restrict__ y, const double* __restrict__ F, const double Fh, double* __restrict__ ydot) {")
+    e.ind += 1
+    e(f"const double T = y[{ns}];")
+    e("const double invT = 1.0 / T;")
+    e("const double lnT = pgb_log(T);")
+    for k in range(ns):
+        e(f"const double C{k} = y[{k}] * {_f(1.0 / W[k])};")
+    emit_gibbs()
+    emit_rates_fp64(True)
+    e("double hs = 0.0, rcp = 0.0;")
+    for k, sp in enumerate(m.species):
+        lf = f"lo_{int(sp.Tmid)}"
+        e(f"{{ const double wm = fma(wd{k}, {_f(W[k])}, F[{k}]); ydot[{k}] = wm;")
+        e(f"  hs = fma({_hW_expr(sp, lf, 1.0 / W[k])}, wm, hs);")
+        e(f"  rcp = fma(y[{k}], {_cpW_expr(sp, lf, R_ERG / W[k])}, rcp); }}")
+    e(f"ydot[{ns}] = fma(-hs, {_f(R_ERG)} * T, Fh) / rcp;")
+    e.ind -= 1
+    e("}")
+    e()
+    # ---------------------------------------------------------------- Jacobian template
+    e("// Analytic Jacobian d ydot / d y in arithmetic type R, written through J(i, k).")
+    e("// Falloff blending factors are held frozen in the [M] and T derivatives.")
+    e("template <class R, class Acc>")
+    e("__device__ __forceinline__ static void jac(const double* __restrict__ y, const double* __restrict__ Fd, const double Fhd, Acc J) {")
+    e.ind += 1
+    e(f"const R T = (R)y[{ns}];")
+    e("const R invT = R(1) / T;")
+    e("const R lnT = pgb_logT<R>(T);")
+    e("const R T2 = T * T, T3 = T2 * T;")
+    for k in range(ns):
+        e(f"const R C{k} = (R)(y[{k}] * {_f(1.0 / W[k])});")
+    # thermo in R
+    tmids = sorted({s.Tmid for s in m.species})
+    for t in tmids:
+        e(f"const bool lo_{int(t)} = T < R({_f(t)});")
+    for k, s in enumerate(m.species):
+        for i in range(7):
+            e(f"const R a{k}_{i} = lo_{int(s.Tmid)} ? R({_f(s.low[i])}) : R({_f(s.high[i])});")
+    e("const R lnT1 = R(1) - lnT;")
+    for k in range(ns):
+        e(f"const R g{k} = a{k}_0 * lnT1 + T * (a{k}_1 * R(-0.5) + T * (a{k}_2 * R(-1.0 / 6.0) + T * (a{k}_3 * R(-1.0 / 12.0) + T * a{k}_4 * R(-0.05)))) + a{k}_5 * invT - a{k}_6;")
+        e(f"const R h{k} = a{k}_0 + T * (a{k}_1 * R(0.5) + T * (a{k}_2 * R(1.0 / 3.0) + T * (a{k}_3 * R(0.25) + T * a{k}_4 * R(0.2)))) + a{k}_5 * invT;")
+        e(f"const R cp{k} = a{k}_0 + T * (a{k}_1 + T * (a{k}_2 + T * (a{k}_3 + T * a{k}_4)));")
+        e(f"const R dcp{k} = a{k}_1 + T * (R(2) * a{k}_2 + T * (R(3) * a{k}_3 + T * R(4) * a{k}_4));")
+    e("for (int i = 0; i < N; ++i)")
+    e("  for (int k = 0; k < N; ++k) J(i, k) = R(0);")
+    needM = any(r.kind != "elementary" for r in m.reactions)
+    if needM:
+        e("const R Ctot = " + " + ".join(f"C{k}" for k in range(ns)) + ";")
+    e(f"const R lnP0RT = R({_f(lnP0_R)}) - lnT;")
+    for k in range(ns):
+        e(f"R wd{k} = R(0);")
+    for k in range(ns):
+        e(f"R dT{k} = R(0);")
+    for j, r in enumerate(m.reactions):
+        e(f"// R{j}: {r.equation()}")
+        e("{")
+        e.ind += 1
+        lnA = math.log(r.rate.A)
+        ear = r.rate.Ea / R_CAL
+        e(f"const R lnkf_inf = R({_f(r.rate.beta)}) * lnT + R({_f(-ear)}) * invT + R({_f(lnA)});")
+        e(f"R dlnkf = (R({_f(r.rate.beta)}) + R({_f(ear)}) * invT) * invT;")
+        if r.kind != "elementary":
+            terms = "Ctot"
+            for sname, eff in r.efficiencies.items():
+                if eff != 1.0:
+                    terms = f"{terms} + R({_f(eff - 1.0)}) * C{idx[sname]}"
+            e(f"const R M = {terms};")
+        if r.kind == "falloff":
+            lnA0 = math.log(r.low.A)
+            ear0 = r.low.Ea / R_CAL
+            e(f"const R lnk0 = R({_f(r.low.beta)}) * lnT + R({_f(-ear0)}) * invT + R({_f(lnA0)});")
+            e(f"const R dlnk0 = (R({_f(r.low.beta)}) + R({_f(ear0)}) * invT) * invT;")
+            e("const R k0 = pgb_expT<R>(lnk0);")
+            e("const R kinf = pgb_expT<R>(lnkf_inf);")
+            e("const R Pr = M * pgb_expT<R>(lnk0 - lnkf_inf);")
+            if r.troe:
+                a, T3, T1 = r.troe[:3]
+                fc = f"R({_f(1.0 - a)}) * pgb_expT<R>(T * R({_f(-1.0 / T3)})) + R({_f(a)}) * pgb_expT<R>(T * R({_f(-1.0 / T1)}))"
+                if len(r.troe) > 3:
+                    fc += f" + pgb_expT<R>(invT * R({_f(-r.troe[3])}))"
+                e(f"const R Fcent = {fc};")
+                e(f"const R lFc = pgb_logT<R>(Fcent) * R({_f(1.0 / LN10)});")
+                e("const R cc = R(-0.4) - R(0.67) * lFc, nn = R(0.75) - R(1.27) * lFc;")
+                e(f"const R lPr = pgb_logT<R>(Pr > R(1e-30) ? Pr : R(1e-30)) * R({_f(1.0 / LN10)}) + cc;")
+                e("const R f1 = lPr / (nn - R(0.14) * lPr);")
+                e(f"const R Fb = pgb_expT<R>(R({_f(LN10)}) * lFc / (R(1) + f1 * f1));")
+            else:
+                e("const R Fb = R(1);")
+            e("const R onePr = R(1) + Pr;")
+            e("const R kf = kinf * Pr / onePr * Fb;")
+            e("const R dkeff_dM = Fb * k0 / (onePr * onePr);")
+            e("dlnkf = dlnkf + (dlnk0 - dlnkf) / onePr;")
+        else:
+            e("const R kf = pgb_expT<R>(lnkf_inf);")
+        pf_f = [idx[s] for s, nu in r.reactants.items() for _ in range(nu)]
+        pr_f = [idx[s] for s, nu in r.products.items() for _ in range(nu)]
+        e("const R Pf = " + " * ".join(f"C{k}" for k in pf_f) + ";")
+        e("const R Pp = " + " * ".join(f"C{k}" for k in pr_f) + ";")
+        dnu = sum(r.products.values()) - sum(r.reactants.values())
+        if r.reversible:
+            dg, dh = [], []
+            for s, nu in r.products.items():
+                dg.append(f"+ R({nu}) * g{idx[s]}")
+                dh.append(f"+ R({nu}) * h{idx[s]}")
+            for s, nu in r.reactants.items():
+                dg.append(f"- R({nu}) * g{idx[s]}")
+                dh.append(f"- R({nu}) * h{idx[s]}")
+            dgs = " ".join(dg)
+            if dnu != 0:
+                dgs += f" - R({dnu}) * lnP0RT"
+            e(f"const R kr = kf * pgb_expT<R>(R(0) {dgs});")
+            e(f"const R dlnkr = dlnkf - (R(0) {' '.join(dh)} - R({dnu})) * invT;")
+        else:
+            e("const R kr = R(0);")
+            e("const R dlnkr = R(0);")
+        alpha = "M" if r.kind == "three_body" else "R(1)"
+        e(f"const R alpha = {alpha};")
+        e("const R q = alpha * (kf * Pf - kr * Pp);")
+        e("const R dqdT = alpha * (kf * dlnkf * Pf - kr * dlnkr * Pp);")
+        # partials dq/dC_k
+        dq: Dict[int, List[str]] = {}
+
+        def partials(side_list, coef):
+            uniq = sorted(set(side_list))
+            for k in uniq:
+                nu = side_list.count(k)
+                others = list(side_list)
+                others.remove(k)
+                term = f"{coef}" + (f" * R({nu})" if nu > 1 else "") + "".join(f" * C{o}" for o in others)
+                dq.setdefault(k, []).append(term)
+
+        partials(pf_f, "alpha * kf")
+        if r.reversible:
+            partials(pr_f, "-alpha * kr")
+        if r.kind == "three_body":
+            e("const R base = kf * Pf - kr * Pp;")
+        elif r.kind == "falloff":
+            e("const R base = dkeff_dM * (Pf - (kf > R(0) ? kr / kf : R(0)) * Pp);")
+        for k, terms in dq.items():
+            e(f"const R dq{k} = " + " + ".join(terms) + ";")
+        nus = {}
+        for s, nu in r.reactants.items():
+            nus[idx[s]] = nus.get(idx[s], 0) - nu
+        for s, nu in r.products.items():
+            nus[idx[s]] = nus.get(idx[s], 0) + nu
+        for i, nu in nus.items():
+            if nu == 0:
+                continue
+            e(f"wd{i} += R({nu}) * q;")
+            e(f"dT{i} += R({nu}) * dqdT;")
+            for k in dq:
+                e(f"J({i}, {k}) += R({_f(nu * W[i] / W[k])}) * dq{k};")
+            if r.kind != "elementary":
+                effs = {idx[s]: eff for s, eff in r.efficiencies.items()}
+                for k in range(ns):
+                    eff = effs.get(k, 1.0)
+                    if eff != 0.0:
+                        e(f"J({i}, {k}) += R({_f(nu * W[i] / W[k] * eff)}) * base;")
+        e.ind -= 1
+        e("}")
+    # temperature column and energy row
+    e("R Dm = R(0), dDm = R(0), Q = (R)Fhd;")
+    for k in range(ns):
+        e(f"const R wm{k} = wd{k} * R({_f(W[k])}) + (R)Fd[{k}];")
+        e(f"const R hm{k} = h{k} * R({_f(R_ERG / W[k])}) * T;")
+        e(f"const R cpm{k} = cp{k} * R({_f(R_ERG / W[k])});")
+        e(f"Dm += (R)y[{k}] * cpm{k};")
+        e(f"dDm += (R)y[{k}] * dcp{k} * R({_f(R_ERG / W[k])});")
+        e(f"Q -= hm{k} * wm{k};")
+        e(f"J({k}, {ns}) = R({_f(W[k])}) * dT{k};")
+    e("const R invD = R(1) / Dm;")
+    e("const R QD2 = Q * invD * invD;")
+    for k in range(ns):
+        terms = " + ".join(f"hm{i} * J({i}, {k})" for i in range(ns))
+        e(f"J({ns}, {k}) = -({terms}) * invD - QD2 * cpm{k};")
+    terms = " + ".join(f"cpm{i} * wm{i} + hm{i} * J({i}, {ns})" for i in range(ns))
+    e(f"J({ns}, {ns}) = -({terms}) * invD - QD2 * dDm;")
+    e.ind -= 1
+    e("}")
+    e.ind -= 1
+    e("};")
+    e("}  // namespace pgb")
+    e(f"#endif  // {guard}")
+    return e.text()
+
+
+def main(outdir: str, names=("lidryer_syn", "drm19_syn", "gri_syn")):
+    from ..workloads import load_mechanism
+    os.makedirs(outdir, exist_ok=True)
+    for n in names:
+        m = load_mechanism(n)
+        text = gen_header(m)
+        path = os.path.join(outdir, f"mech_{n}.cuh")
+        if os.path.exists(path):
+            with open(path) as f:
+                if f.read() == text:
+                    continue  # unchanged: keep the timestamp so the library is not rebuilt
+        with open(path, "w") as f:
+            f.write(text)
+
+
+if __name__ == "__main__":
+    import sys
+    here = os.path.dirname(os.path.abspath(__file__))
+    main(sys.argv[1] if len(sys.argv) > 1 else os.path.join(here, "..", "csrc", "gen"))

@@ -46,11 +46,13 @@ def species_h_mass(mech: Mechanism, T: np.ndarray) -> np.ndarray:
     """h_k(T) [erg/g], shape (ncell, ns)."""
     lo, hi, tm, W = _coeffs(mech)
     T = np.asarray(T, dtype=float)[:, None]
-    a = np.where(T < tm[None, :], 1.0, 0.0)[..., None] * lo[None] + \
-        np.where(T < tm[None, :], 0.0, 1.0)[..., None] * hi[None]
-    hRT = (a[..., 0] + a[..., 1] * T / 2 + a[..., 2] * T ** 2 / 3 + a[..., 3] * T ** 3 / 4
-           + a[..., 4] * T ** 4 / 5 + a[..., 5] / T)
-    return hRT * R_ERG * T / W[None, :]
+
+    def hRT(a):
+        return (a[None, :, 0] + a[None, :, 1] * T / 2 + a[None, :, 2] * T ** 2 / 3 + a[None, :, 3] * T ** 3 / 4
+                + a[None, :, 4] * T ** 4 / 5 + a[None, :, 5] / T)
+
+    h = np.where(T < tm[None, :], hRT(lo), hRT(hi))
+    return h * R_ERG * T / W[None, :]
 
 
 def mixture_h(mech: Mechanism, T: np.ndarray, Y: np.ndarray) -> np.ndarray:

@@ -1,0 +1,165 @@
+"""GPU parity: the GB300 reactor (through the C ABI) against the CPU oracle on the same seeded
+inputs.
+
+Tolerances are the ones the benchmark definition states for the plain method at
+ode.rtol / ode.atol: temperature within 1e-6 relative, every rhoY within atol + rtol*|rhoY|.
+Both sides run the same CVODE-class algorithm, so these hold cell by cell; rho h must match to
+round-off (it is rho h0 + F_h dt on both sides).
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from helpers import boxes_from_cells, gather, tol_ratio
+from pelelm_gb300.reactor import ReactorBase
+from pelelm_gb300.workloads import CONFIGS, make_cells, mech_path
+
+OUT = os.environ.get("PGB_TEST_OUT", "gpurun_out")
+
+
+def _report(name, d):
+    try:
+        os.makedirs(OUT, exist_ok=True)
+        with open(os.path.join(OUT, "parity_report.jsonl"), "a") as f:
+            f.write(json.dumps({"test": name, **d}) + "\n")
+    except OSError:
+        pass
+
+
+def _run_both(torch, oracle_mod, cfg, n, seed, precision, sides):
+    cs = make_cells(cfg, n, seed=seed)
+    boxes = boxes_from_cells(torch, cs, sides)
+    r = ReactorBase.create("ReactorCvode", cfg.mech,
+                           f"ode.rtol={cfg.rtol} ode.atol={cfg.atol} gb.precision={precision}")
+    r.init(2, 1)
+    nfail = 0
+    for b in boxes:
+        nfail += r.react(b.box, b.rY, b.rY_src, b.T, b.rEner, b.rEner_src, b.FC, b.mask, cfg.dt, 0.0)
+    torch.cuda.synchronize()
+    g = gather(boxes, cs.rY.shape[1])
+    om = oracle_mod.OracleMech(mech_path(cfg.mech))
+    o = om.react(cs.rY, cs.rYsrc, cs.T, cs.rE, cs.rEsrc, cs.mask, cfg.dt, cfg.rtol, cfg.atol)
+    r.close()
+    return cs, g, o, nfail
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("cfgname,n,sides", [("lidryer_32cube", 4096, [16]),
+                                             ("lidryer_amr120", 2048, [8, 8, 8, 8])])
+def test_react_fp64_matches_oracle(native_lib, oracle_mod, cuda, cfgname, n, sides):
+    """Plain method (FP64 Jacobian and LU) against the oracle at the same rtol/atol."""
+    precision = "fp64"
+    torch = cuda
+    cfg = CONFIGS[cfgname]
+    cs, g, o, nfail = _run_both(torch, oracle_mod, cfg, n, 7, precision, sides)
+    rYg, Tg, rEg, FCg = g
+    rYo, To, rEo, FCo, nfail_o = o
+    relT = np.abs(Tg - To) / To
+    ratio = tol_ratio(rYg, rYo, cfg.rtol, cfg.atol)
+    same_nfe = float(np.mean(FCg == FCo))
+    _report(f"react[{cfgname},{precision}]", {
+        "max_relT": float(relT.max()), "p99_relT": float(np.percentile(relT, 99)),
+        "max_ratio": float(ratio.max()), "p99_ratio": float(np.percentile(ratio, 99)),
+        "frac_same_nfe": same_nfe, "nfe_gpu": float(FCg.mean()), "nfe_orc": float(FCo.mean()),
+        "nfail": int(nfail), "nfail_oracle": int(nfail_o)})
+    assert nfail == 0 and nfail_o == 0
+    assert np.all(FCg > 0)
+    np.testing.assert_allclose(rEg, rEo, rtol=1e-14, atol=0)
+    assert relT.max() <= 1e-6, f"T rel err {relT.max():.3e}"
+    assert ratio.max() <= 1.0, f"rhoY err / (atol + rtol|rhoY|) = {ratio.max():.3e}"
+    # same algorithm in the same precision: step/RHS counts agree on almost every cell
+    assert same_nfe >= 0.9
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("cfgname,n,sides", [("lidryer_32cube", 4096, [16]),
+                                             ("lidryer_amr120", 2048, [8, 8, 8, 8])])
+def test_react_mixed_accuracy_vs_tight_oracle(native_lib, oracle_mod, cuda, cfgname, n, sides):
+    """Mixed precision (FP32 Jacobian/LU preconditioner, FP64 rates, residual, error test and
+    step control) takes different Newton iterates than the FP64 path, so it is judged the way
+    the benchmark definition asks: by its error against a tight-tolerance oracle (rtol 1e-11),
+    which must be no worse than the error the plain FP64 oracle itself makes at the same
+    rtol/atol (max and 99th percentile, T and mass fractions; 25% slack plus 1e-3 K / 1e-8)."""
+    torch = cuda
+    cfg = CONFIGS[cfgname]
+    cs, g, o, nfail = _run_both(torch, oracle_mod, cfg, n, 7, "mixed", sides)
+    om = oracle_mod.OracleMech(mech_path(cfg.mech))
+    tight = om.react(cs.rY, cs.rYsrc, cs.T, cs.rE, cs.rEsrc, cs.mask, cfg.dt, 1e-11, 1e-16,
+                     max_steps=200000)
+    Yt = tight[0] / tight[0].sum(1, keepdims=True)
+
+    def errs(rY, T):
+        Y = rY / rY.sum(1, keepdims=True)
+        dT = np.abs(T - tight[1])
+        dY = np.abs(Y - Yt).max(1)
+        return dT.max(), np.percentile(dT, 99), dY.max(), np.percentile(dY, 99)
+
+    em = errs(g[0], g[1])
+    eo = errs(o[0], o[1])
+    _report(f"mixed_vs_tight[{cfgname}]", {"mixed": [float(x) for x in em],
+                                           "oracle_same_rtol": [float(x) for x in eo]})
+    assert nfail == 0
+    for a, b, slack in zip(em, eo, (1e-3, 1e-3, 1e-8, 1e-8)):
+        assert a <= 1.25 * b + slack, (em, eo)
+
+
+@pytest.mark.gpu
+def test_react_boxes_ghosts_offsets_mask_graph(native_lib, oracle_mod, cuda):
+    """Several boxes (uneven sizes, non-zero lo, ghost cells, a mask) in one persistent launch,
+    also replayed from a captured CUDA graph; covered cells keep their state and get FC = 0."""
+    torch = cuda
+    cfg = CONFIGS["lidryer_amr120"]
+    shapes = [(8, 8, 8), (16, 4, 8), (5, 7, 3), (12, 6, 4)]
+    n = sum(a * b * c for a, b, c in shapes)
+    cs = make_cells(cfg, n, seed=3)
+    rng = np.random.default_rng(5)
+    cs.mask[:] = np.where(rng.uniform(size=n) < 0.1, -1, 1)
+    los = [(0, 0, 0), (8, -4, 2), (-3, 5, 100), (40, 40, 40)]
+    stream = torch.cuda.Stream()
+    for graph in (0, 1):
+        boxes = boxes_from_cells(torch, cs, shapes, lo_list=los, ghost=2, with_mask=True)
+        r = ReactorBase.create("ReactorCvode", cfg.mech,
+                               f"ode.rtol={cfg.rtol} ode.atol={cfg.atol} gb.graph={graph} "
+                               "gb.precision=fp64")
+        r.init(2, 1)
+        with torch.cuda.stream(stream):
+            r.react_boxes(boxes, cfg.dt, 0.0, stream=stream)
+            if graph:  # second replay of the captured graph on fresh inputs
+                boxes = boxes_from_cells(torch, cs, shapes, lo_list=los, ghost=2, with_mask=True)
+                r.react_boxes(boxes, cfg.dt, 0.0, stream=stream)
+        st = r.stats()
+        stream.synchronize()
+        rYg, Tg, rEg, FCg = gather(boxes, cs.rY.shape[1])
+        om = oracle_mod.OracleMech(mech_path(cfg.mech))
+        rYo, To, rEo, FCo, nf = om.react(cs.rY, cs.rYsrc, cs.T, cs.rE, cs.rEsrc, cs.mask, cfg.dt,
+                                         cfg.rtol, cfg.atol)
+        covered = cs.mask < 0
+        assert st["nfail"] == 0 and nf == 0
+        assert st["ncell"] == n
+        assert np.all(FCg[covered] == 0) and np.all(FCg[~covered] > 0)
+        np.testing.assert_array_equal(Tg[covered], cs.T[covered])
+        np.testing.assert_array_equal(rYg[covered], cs.rY[covered])
+        relT = np.abs(Tg - To) / To
+        assert relT.max() <= 1e-6
+        assert tol_ratio(rYg, rYo, cfg.rtol, cfg.atol).max() <= 1.0
+        r.close()
+
+
+@pytest.mark.gpu
+def test_null_reactor(native_lib, cuda):
+    """ReactorNull advances the forcing only: rhoY += dt F, rho h += dt F_h, FC = 0."""
+    torch = cuda
+    cfg = CONFIGS["lidryer_amr120"]
+    cs = make_cells(cfg, 512, seed=9)
+    boxes = boxes_from_cells(torch, cs, [8])
+    r = ReactorBase.create("ReactorNull", cfg.mech, "")
+    r.init(2, 1)
+    b = boxes[0]
+    assert r.react(b.box, b.rY, b.rY_src, b.T, b.rEner, b.rEner_src, b.FC, None, cfg.dt, 0.0) == 0
+    rYg, Tg, rEg, FCg = gather(boxes, cs.rY.shape[1])
+    np.testing.assert_allclose(rYg, cs.rY + cfg.dt * cs.rYsrc, rtol=1e-14, atol=1e-30)
+    np.testing.assert_allclose(rEg, cs.rE + cfg.dt * cs.rEsrc, rtol=1e-14)
+    assert np.all(FCg == 0)
+    r.close()
