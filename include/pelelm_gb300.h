@@ -114,6 +114,30 @@ int pgb_reaction_rates(const char* mechanism, const pgb_box_view* view, const pg
 int pgb_rhoh_to_temp(const char* mechanism, const pgb_box_view* view, double tmin, double tmax,
                      void* stream);
 
+/* Allocation-free advance of up to PGB_NOALLOC_MAX_BOXES boxes, for callers that cannot
+ * allocate device memory at react time. No counterpart in the reference. PeleLM, for example,
+ * runs on an AMReX arena that reserves most of the GPU at start-up, so a cudaMalloc issued by
+ * the reactor in the middle of a time step can fail or fragment what the arena left, and
+ * cudaMalloc/cudaFree can synchronize the device. This entry point allocates nothing — no
+ * cudaMalloc, cudaFree or other allocating routine: the caller passes all inputs and outputs
+ * through the box views, and the scratch (box table, work-queue head, counters) is one fixed
+ * device array inside the library, about 370 KB, which every GPU that loads the library holds
+ * until the process exits. It runs the same persistent work-stealing kernel as
+ * pgb_reactor_react_boxes with uniform tolerances (rtol, atol), cvode.max_order = max_order,
+ * ode.max_steps = max_steps and FP64 (fp64 != 0) or mixed (fp64 == 0) Jacobian precision.
+ * - nbox must be in [1, PGB_NOALLOC_MAX_BOXES]; larger box lists are rejected with an error.
+ * - The first call on a device (with that device current) resolves the scratch array's device
+ *   address; make that first call before any stream capture.
+ * - All calls on a device share the one scratch array, which keeps the last call's contents
+ *   (the queue head and counters are cleared on each call). Calls whose work overlaps on the
+ *   GPU — concurrent streams or threads — race on it: serialize them.
+ * - Stream ordered; if stats is non-NULL the call waits for the advance and fills it.
+ * Returns 0 on success, -1 on error (pgb_last_error). */
+#define PGB_NOALLOC_MAX_BOXES 1024
+int pgb_react_boxes_noalloc(const char* mechanism, const pgb_box_view* views, int nbox,
+                            double dt_react, double rtol, double atol, int max_order, int max_steps,
+                            int fp64, void* stream, pgb_stats* stats);
+
 /* Measures the device's FP64 FMA throughput in TFLOP/s (2 flops per FMA). No counterpart in
  * the reference: a measurement utility giving the roofline denominator of the FP64-bound
  * reactor kernels. */

@@ -49,6 +49,9 @@ EXPORTS = {
     "pgb_reaction_rates": (C.c_int, [C.c_char_p, C.POINTER(BoxView), C.POINTER(Array4), _vp]),
     "pgb_rhoh_to_temp": (C.c_int, [C.c_char_p, C.POINTER(BoxView), C.c_double, C.c_double, _vp]),
     "pgb_fp64_peak_tflops": (C.c_int, [C.c_int, C.POINTER(C.c_double)]),
+    "pgb_react_boxes_noalloc": (C.c_int, [C.c_char_p, C.POINTER(BoxView), C.c_int, C.c_double,
+                                          C.c_double, C.c_double, C.c_int, C.c_int, C.c_int, _vp,
+                                          C.POINTER(Stats)]),
 }
 
 _lib = None

@@ -422,3 +422,5 @@ const MechEntry* find_mech(const char* name) {
 }
 
 }  // namespace
+
+const pgb_host::MechEntry* pgb_host::find_mech_entry(const char* name) { return find_mech(name); }

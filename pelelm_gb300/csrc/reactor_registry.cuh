@@ -138,6 +138,41 @@ int h2t_entry(const pgb_box_view* v, double tmin, double tmax, cudaStream_t s) {
         ::pgb_host::h2t_entry<M>                                                             \
   }
 
+// Converts and validates one box view into its device descriptor; cell numbering of the box
+// starts at cell_offset.
+inline int fill_box_dev(const pgb_box_view& v, int ns, long long cell_offset, int ibox,
+                        pgb::BoxDev& d) {
+  const pgb_box& bx = v.box;
+  for (int k = 0; k < 3; ++k)
+    if (bx.hi[k] < bx.lo[k]) return set_err("box %d is empty in dim %d", ibox, k);
+  if (check_arr(v.rY, bx, ns, "rY", ibox) || check_arr(v.rY_src, bx, ns, "rY_src", ibox) ||
+      check_arr(v.T, bx, 1, "T", ibox) || check_arr(v.rEner, bx, 1, "rEner", ibox) ||
+      check_arr(v.rEner_src, bx, 1, "rEner_src", ibox) || check_arr(v.FC, bx, 1, "FC", ibox))
+    return -1;
+  if (v.mask.p && check_arr(v.mask, bx, 1, "mask", ibox)) return -1;
+  d.lo0 = bx.lo[0]; d.lo1 = bx.lo[1]; d.lo2 = bx.lo[2];
+  d.len0 = bx.hi[0] - bx.lo[0] + 1;
+  d.len1 = bx.hi[1] - bx.lo[1] + 1;
+  d.len2 = bx.hi[2] - bx.lo[2] + 1;
+  d.cell_offset = cell_offset;
+  d.rY = arr_dev(v.rY);
+  d.rYsrc = arr_dev(v.rY_src);
+  d.T = arr_dev(v.T);
+  d.rE = arr_dev(v.rEner);
+  d.rEsrc = arr_dev(v.rEner_src);
+  d.FC = arr_dev(v.FC);
+  d.mask.p = static_cast<const int*>(v.mask.p);
+  d.mask.jstride = v.mask.jstride;
+  d.mask.kstride = v.mask.kstride;
+  d.mask.begin0 = v.mask.begin[0];
+  d.mask.begin1 = v.mask.begin[1];
+  d.mask.begin2 = v.mask.begin[2];
+  return 0;
+}
+
+// Registry lookup by mechanism name (nullptr when the mechanism is not compiled in).
+const MechEntry* find_mech_entry(const char* name);
+
 }  // namespace pgb_host
 
 #endif  // PGB_REACTOR_REGISTRY_CUH

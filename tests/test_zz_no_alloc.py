@@ -1,0 +1,78 @@
+"""The allocation-free entry point (pgb_react_boxes_noalloc) against the allocating one.
+
+Callers such as PeleLM run on an AMReX arena that reserves most of the GPU up front; they need
+a reactor call that allocates no device memory. This test drives that entry point through the
+C ABI twice in a row (the fixed scratch array keeps the previous call's contents, so the second
+call checks that the queue head and counters are cleared) and compares every output with
+pgb_reactor_react_boxes on the same inputs, within the parity tolerances the other tests use
+(T within 1e-6 relative, rhoY within atol + rtol |rhoY|). It is collected last so that a run
+stopping at the first failure has already run every other test.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from helpers import boxes_from_cells, gather, tol_ratio
+from pelelm_gb300 import _lib
+from pelelm_gb300.reactor import ReactorBase
+from pelelm_gb300.workloads import CONFIGS, make_cells
+
+SHAPES = [(8, 8, 8), (16, 4, 8), (5, 7, 3), (12, 6, 4)]
+LOS = [(0, 0, 0), (8, -4, 2), (-3, 5, 100), (40, 40, 40)]
+
+
+def _inputs():
+    cfg = CONFIGS["lidryer_amr120"]
+    n = sum(a * b * c for a, b, c in SHAPES)
+    cs = make_cells(cfg, n, seed=17)
+    rng = np.random.default_rng(2)
+    cs.mask[:] = np.where(rng.uniform(size=n) < 0.1, -1, 1)
+    return cfg, cs
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_noalloc_matches_allocating_entry(native_lib, cuda, precision):
+    torch = cuda
+    cfg, cs = _inputs()
+    ns = cs.rY.shape[1]
+    lib = _lib.lib()
+
+    # reference: the allocating multi-box entry point
+    boxes = boxes_from_cells(torch, cs, SHAPES, lo_list=LOS, ghost=1, with_mask=True)
+    r = ReactorBase.create("ReactorCvode", cfg.mech,
+                           f"ode.rtol={cfg.rtol} ode.atol={cfg.atol} gb.precision={precision}")
+    r.init(2, 1)
+    r.react_boxes(boxes, cfg.dt, 0.0)
+    st_ref = r.stats()
+    r.close()
+    ref = gather(boxes, ns)
+
+    for call in range(2):
+        boxes = boxes_from_cells(torch, cs, SHAPES, lo_list=LOS, ghost=1, with_mask=True)
+        views = (_lib.BoxView * len(boxes))(*[b.view() for b in boxes])
+        st = _lib.Stats()
+        rc = lib.pgb_react_boxes_noalloc(cfg.mech.encode(), views, len(boxes), cfg.dt, cfg.rtol,
+                                         cfg.atol, 5, 20000, int(precision == "fp64"), None,
+                                         C.byref(st))
+        assert rc == 0, _lib.last_error()
+        torch.cuda.synchronize()
+        rY, T, rE, FC = gather(boxes, ns)
+        assert st.nfail == 0 and st.ncell == st_ref["ncell"]
+        assert st.nfe == st_ref["nfe"], f"call {call}: RHS counts differ"
+        np.testing.assert_array_equal(FC, ref[3])
+        assert np.max(np.abs(T - ref[1]) / ref[1]) <= 1e-6
+        assert tol_ratio(rY, ref[0], cfg.rtol, cfg.atol).max() <= 1.0
+        np.testing.assert_allclose(rE, ref[2], rtol=1e-14)
+
+
+@pytest.mark.gpu
+def test_noalloc_rejects_too_many_boxes(native_lib, cuda):
+    cfg, _ = _inputs()
+    n = 1025  # one more than PGB_NOALLOC_MAX_BOXES
+    views = (_lib.BoxView * n)()
+    rc = _lib.lib().pgb_react_boxes_noalloc(cfg.mech.encode(), views, n, cfg.dt, cfg.rtol, cfg.atol,
+                                            5, 20000, 1, None, None)
+    assert rc == -1
+    assert "exceed" in _lib.last_error()
