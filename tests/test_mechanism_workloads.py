@@ -1,0 +1,89 @@
+"""Mechanism generator invariants, generated-code inputs and benchmark workload definitions."""
+import numpy as np
+import pytest
+
+from pelelm_gb300.mech.generate import DRM19_SPECIES, LIDRYER_SPECIES, generate
+from pelelm_gb300.mech.model import Mechanism
+from pelelm_gb300.workloads import (CONFIGS, box_layout, from_box_arena, load_mechanism, make_cells,
+                                    mech_path, to_box_arena)
+
+SHAPES = {"lidryer_syn": (9, 21), "drm19_syn": (21, 84), "gri_syn": (53, 325)}
+
+
+@pytest.mark.parametrize("name", list(SHAPES))
+def test_shapes_and_element_balance(name):
+    m = load_mechanism(name)
+    assert (m.ns, m.nr) == SHAPES[name]
+    assert m.synthetic
+    for r in m.reactions:
+        bal = {}
+        for side, sign in ((r.reactants, -1), (r.products, 1)):
+            for s, nu in side.items():
+                for e, n in m.species[m.index(s)].composition.items():
+                    bal[e] = bal.get(e, 0) + sign * nu * n
+        assert all(v == 0 for v in bal.values()), r.equation()
+
+
+def test_species_orders_follow_reference_fixtures():
+    assert [s.name for s in load_mechanism("lidryer_syn").species] == LIDRYER_SPECIES
+    assert [s.name for s in load_mechanism("drm19_syn").species] == DRM19_SPECIES
+
+
+@pytest.mark.parametrize("name", list(SHAPES))
+def test_thermo_continuous_at_tmid(name):
+    m = load_mechanism(name)
+    for s in m.species:
+        T = s.Tmid
+        for a_lo, a_hi in ((s.low, s.high),):
+            def cp(a):
+                return a[0] + a[1] * T + a[2] * T ** 2 + a[3] * T ** 3 + a[4] * T ** 4
+
+            def h(a):
+                return a[0] + a[1] * T / 2 + a[2] * T ** 2 / 3 + a[3] * T ** 3 / 4 + a[4] * T ** 4 / 5 + a[5] / T
+
+            def sR(a):
+                return a[0] * np.log(T) + a[1] * T + a[2] * T ** 2 / 2 + a[3] * T ** 3 / 3 + a[4] * T ** 4 / 4 + a[6]
+            assert abs(cp(a_lo) - cp(a_hi)) < 1e-9 * abs(cp(a_lo))
+            assert abs(h(a_lo) - h(a_hi)) < 1e-9 * (abs(h(a_lo)) + 1)
+            assert abs(sR(a_lo) - sR(a_hi)) < 1e-9 * (abs(sR(a_lo)) + 1)
+
+
+def test_generator_is_deterministic(tmp_path):
+    a = generate("lidryer_syn")
+    p = tmp_path / "x.json"
+    a.to_json(str(p))
+    b = Mechanism.from_json(str(p))
+    committed = load_mechanism("lidryer_syn")
+    assert [r.equation() for r in b.reactions] == [r.equation() for r in committed.reactions]
+    np.testing.assert_allclose([r.rate.A for r in b.reactions], [r.rate.A for r in committed.reactions])
+
+
+def test_flat_file_matches_json(tmp_path):
+    m = load_mechanism("drm19_syn")
+    p = tmp_path / "d.mech"
+    m.to_flat(str(p))
+    assert p.read_text() == open(mech_path("drm19_syn")).read()
+
+
+def test_amr_workload_definition():
+    cfg = CONFIGS["lidryer_amr120"]
+    assert len(cfg.boxes) == 120 and cfg.ncell == 2154496
+    assert set(cfg.boxes) == {8, 16, 32, 64}
+    assert CONFIGS["lidryer_32cube"].ncell == 32768
+    assert CONFIGS["drm19_2M"].ncell == 2 ** 21
+    assert CONFIGS["gri_1M"].ncell == 2 ** 20
+
+
+def test_forcing_is_realizable_and_mass_neutral():
+    cfg = CONFIGS["lidryer_amr120"]
+    cs = make_cells(cfg, 5000, seed=3)
+    assert np.allclose(cs.rYsrc.sum(axis=1), 0.0, atol=1e-12 * np.abs(cs.rYsrc).max())
+    assert np.all(cs.rY + cfg.dt * cs.rYsrc >= 0.0)  # species absent at t=0 get no sink
+    assert 0.0 < np.std(cs.rYsrc) < 1.0
+    assert np.all((cs.T >= 300) & (cs.T <= 2400))
+
+
+def test_box_arena_roundtrip():
+    lay = box_layout([4, 2, 3])
+    a = np.random.default_rng(0).normal(size=(lay.ncell, 5))
+    np.testing.assert_array_equal(from_box_arena(lay, to_box_arena(lay, a), 5), a)
