@@ -40,30 +40,51 @@ constexpr int MAXCOR = 3, MSBP = 20;
 constexpr double CRDOWN = 0.3, RDIV = 2.0, DGMAX = 0.3, NLSCOEF = 0.1;
 
 enum Phase : int { IDLE = 0, NEED = 1, START = 2, HIN = 3, STEP = 4, NEWTON = 5, RESETD = 6 };
+
+// 1/j for the small integers the order logic divides by (no FP64 division on the device)
+__device__ __forceinline__ double inv_int(int j) {
+  return j == 1 ? 1.0 : j == 2 ? 0.5 : j == 3 ? 1.0 / 3.0 : j == 4 ? 0.25 : j == 5 ? 0.2
+       : j == 6 ? 1.0 / 6.0 : 1.0 / 7.0;
+}
+
+// 1/x to ~1e-14 from an FP32 seed and one Newton step (3 FP64-pipe instructions instead of a
+// 7-8 slot IEEE division); used for error weights in mixed precision. x must lie in the
+// normal FP32 range.
+__device__ __forceinline__ double recip_fast(double x) {
+  const double y0 = (double)__frcp_rn((float)x);
+  return fma(y0, fma(-x, y0, 1.0), y0);
+}
 enum Status : int { OK = 0, MAX_STEPS = 1, ERRTEST = 2, CONV = 3, HSMALL = 4, NONFINITE = 5 };
 }  // namespace bdf
 
-// Bytes of dynamic shared memory per thread for mechanism M with Jacobian type JR.
-template <class M, class JR>
+// Bytes of dynamic shared memory per thread for mechanism M with Jacobian type JR; the
+// Jacobian/LU slice lives in shared memory unless LU_GLOBAL (then in the L2-resident global
+// scratch ReactParams::lu_scratch, one [N*N][slot] array over all resident threads).
+template <class M, class JR, bool LU_GLOBAL = false>
 __host__ __device__ constexpr int bdf_smem_per_thread() {
   return (QMAX + 2) * M::N * 8    // Nordsieck z[0..QMAX] + saved correction
          + (QMAX + 1) * 8         // l coefficients
          + (QMAX + 2) * 8         // step history tau
          + M::N * 8               // forcing (F_rhoY, F_rhoh)
-         + M::N * M::N * (int)sizeof(JR)  // Jacobian / LU
+         + M::N * (int)sizeof(JR)  // triangular-solve vector
+         + (LU_GLOBAL ? 0 : M::N * M::N * (int)sizeof(JR))  // Jacobian / LU
          + ((M::N + 7) / 8) * 8;  // pivots
 }
 
-template <class JR, int TPB>
-struct LuAcc {  // J(i,k) view of the per-thread matrix slice
+template <class JR>
+struct LuAcc {  // J(i,k) view of one thread's matrix slice, element stride `stride`
   JR* base;
   int n;
-  __device__ __forceinline__ JR& operator()(int i, int k) const { return base[(i * n + k) * TPB]; }
+  long long stride;
+  __device__ __forceinline__ JR& operator()(int i, int k) const {
+    return base[(long long)(i * n + k) * stride];
+  }
 };
 
-template <class M, class JR, int TPB>
+template <class M, class JR, int TPB, bool LU_GLOBAL = false>
 __global__ void __launch_bounds__(TPB, 1) bdf_reactor_kernel(const ReactParams P) {
   using namespace bdf;
+  constexpr bool MIXED = sizeof(JR) == sizeof(float);
   constexpr int N = M::N;
   constexpr int NS = M::NS;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -73,14 +94,21 @@ __global__ void __launch_bounds__(TPB, 1) bdf_reactor_kernel(const ReactParams P
   double* Ls = Zs + (QMAX + 2) * N * TPB;                      // [QMAX+1][TPB]
   double* TAUs = Ls + (QMAX + 1) * TPB;                        // [QMAX+2][TPB]
   double* Fs = TAUs + (QMAX + 2) * TPB;                        // [N][TPB]
-  JR* LUs = reinterpret_cast<JR*>(Fs + N * TPB);               // [N*N][TPB]
-  unsigned char* PIVs = reinterpret_cast<unsigned char*>(LUs + N * N * TPB);  // [N][TPB]
+  JR* XSs = reinterpret_cast<JR*>(Fs + N * TPB);               // [N][TPB] solve vector
+  JR* LUs = XSs + N * TPB;                                      // [N*N][TPB] (shared variant)
+  unsigned char* PIVs =
+      reinterpret_cast<unsigned char*>(LU_GLOBAL ? reinterpret_cast<JR*>(LUs) : LUs + N * N * TPB);  // [N][TPB]
+  // this thread's Jacobian / LU slice and its element stride
+  JR* const LUb = LU_GLOBAL ? static_cast<JR*>(P.lu_scratch) + (long long)blockIdx.x * TPB + tid
+                            : LUs + tid;
+  const long long lu_stride = LU_GLOBAL ? (long long)gridDim.x * TPB : (long long)TPB;
 #define Z(j, i) Zs[((j) * N + (i)) * TPB + tid]
 #define LCO(j) Ls[(j) * TPB + tid]
 #define TAU(j) TAUs[(j) * TPB + tid]
 #define FRC(i) Fs[(i) * TPB + tid]
-#define LU(i, k) LUs[((i) * N + (k)) * TPB + tid]
+#define LU(i, k) LUb[(long long)((i) * N + (k)) * lu_stride]
 #define PIV(k) PIVs[(k) * TPB + tid]
+#define XS(i) XSs[(i) * TPB + tid]
   const int qmax = max(1, min(P.max_order, QMAX));
   const double tout = P.dt;
 
@@ -90,9 +118,11 @@ __global__ void __launch_bounds__(TPB, 1) bdf_reactor_kernel(const ReactParams P
   int box = 0, ci = 0, cj = 0, ck = 0;
   double y[N], acor[N], ewt[N];
   double t = 0.0, h = 0.0, hscale = 0.0, etamax = ETAMX1, eta = 1.0;
-  double gamma = 0.0, gammap = 0.0, gamrat = 1.0, crate = 1.0, rl1 = 1.0;
-  double tq1 = 1.0, tq2 = 1.0, tq3 = 1.0, tq4 = 1.0, tq5 = 1.0, tq5_saved = 1.0;
-  double del = 0.0, delp = 0.0, hg = 0.0, hub = 0.0, hlb = 0.0, rE0 = 0.0;
+  double gamma = 0.0, gammap = 0.0, gamrat = 1.0, crate2 = 1.0, rl1 = 1.0;
+  // tq1..tq5: error constants; the Newton test constant tq4 = NLSCOEF/tq2 is kept as 1/tq4^2
+  double tq1 = 1.0, tq2 = 1.0, tq3 = 1.0, tq5 = 1.0, tq5_saved = 1.0, inv_tq4_sq = 1.0;
+  // del2/delp2: squared WRMS norms of the last / previous Newton corrections; crate2 = crate^2
+  double del2 = 0.0, delp2 = 0.0, hg = 0.0, hub = 0.0, hlb = 0.0, rE0 = 0.0;
   int q = 1, qwait = 2, nef = 0, ncf = 0, m = 0, hin_count = 0, status = OK;
   long long nst = 0, nfe = 0, nje = 0, nstlp = 0, netf = 0, ncfn = 0;
   bool new_step = true, need_setup = true, force_setup = true, jcur = false;
@@ -100,15 +130,20 @@ __global__ void __launch_bounds__(TPB, 1) bdf_reactor_kernel(const ReactParams P
 #pragma unroll
   for (int i = 0; i < N; ++i) { y[i] = 0.0; acor[i] = 0.0; ewt[i] = 1.0; }
 
-  auto wrms = [&](const double* v) -> double {
+  // weighted mean square (the square of CVODE's WRMS norm): every test below compares squares,
+  // so no FP64 square root is taken on the step path
+  auto wms = [&](const double* v) -> double {
     double s = 0.0;
 #pragma unroll
     for (int i = 0; i < N; ++i) { const double x = v[i] * ewt[i]; s = fma(x, x, s); }
-    return sqrt(s * (1.0 / N));
+    return s * (1.0 / N);
   };
   auto set_ewt = [&]() {
 #pragma unroll
-    for (int i = 0; i < N; ++i) ewt[i] = 1.0 / fma(P.rtol, fabs(Z(0, i)), P.atol[i]);
+    for (int i = 0; i < N; ++i) {
+      const double d = fma(P.rtol, fabs(Z(0, i)), P.atol[i]);
+      ewt[i] = MIXED ? recip_fast(d) : 1.0 / d;
+    }
   };
   auto rescale = [&](double e) {
     double fac = e;
@@ -141,7 +176,7 @@ __global__ void __launch_bounds__(TPB, 1) bdf_reactor_kernel(const ReactParams P
     for (int i = 0; i <= qmax; ++i) LCO(i) = 0.0;
     LCO(0) = 1.0;
     double alpha0 = 0.0;
-    for (int j = 1; j <= q; ++j) alpha0 -= 1.0 / j;
+    for (int j = 1; j <= q; ++j) alpha0 -= inv_int(j);
     double hsum = h, sum_xi_inv = 0.0;
     for (int i = 1; i <= q - 1; ++i) {
       if (i > 1) hsum += TAU(i - 1);
@@ -161,19 +196,19 @@ __global__ void __launch_bounds__(TPB, 1) bdf_reactor_kernel(const ReactParams P
     if (qwait == 1) {
       if (q > 1) {
         const double C = xistar_inv / LCO(q);
-        const double A3 = alpha0 + 1.0 / q;
+        const double A3 = alpha0 + inv_int(q);
         const double A4 = alpha0_hat + xiq_inv;
         tq1 = fabs(C * (1.0 - A4 + A3) / A3);
       } else {
         tq1 = 1.0;
       }
       const double xiq1_inv = h / (hsum + TAU(q));
-      const double A5 = alpha0 - 1.0 / (q + 1);
+      const double A5 = alpha0 - inv_int(q + 1);
       const double A6 = alpha0_hat - xiq1_inv;
       const double Cpp = (1.0 - A6 + A5) / A2;
       tq3 = fabs(Cpp / (xiq1_inv * (q + 2) * A5));
     }
-    tq4 = NLSCOEF / tq2;
+    inv_tq4_sq = (tq2 * (1.0 / NLSCOEF)) * (tq2 * (1.0 / NLSCOEF));
   };
   auto adjust_order = [&](int dq) {
     double w[QMAX + 2];
@@ -185,7 +220,7 @@ __global__ void __launch_bounds__(TPB, 1) bdf_reactor_kernel(const ReactParams P
         hsum += TAU(j);
         const double xi = hsum / hscale;
         prod *= xi;
-        alpha0 -= 1.0 / j;
+        alpha0 -= inv_int(j);
         alpha1 += 1.0 / xi;
         if (j <= q - 1)
           for (int i = j + 2; i >= 2; --i) w[i] = w[i] * xi + w[i - 1];
@@ -216,15 +251,18 @@ __global__ void __launch_bounds__(TPB, 1) bdf_reactor_kernel(const ReactParams P
   };
   // M = I - gamma J in the LU slice, factor with partial pivoting (trailing swaps)
   auto setup_matrix = [&]() -> bool {
-    LuAcc<JR, TPB> acc{&LUs[tid], N};
+    LuAcc<JR> acc{LUb, N, lu_stride};
     double Fl[NS];
 #pragma unroll
     for (int i = 0; i < NS; ++i) Fl[i] = FRC(i);
     M::template jac<JR>(y, Fl, FRC(NS), acc);
     const JR g = (JR)gamma;
+#pragma unroll 1
     for (int i = 0; i < N; ++i)
       for (int k = 0; k < N; ++k) LU(i, k) = (i == k ? JR(1) : JR(0)) - g * LU(i, k);
     bool ok = true;
+    // partial-pivot LU; the diagonal keeps the reciprocal pivot for the solve
+#pragma unroll 1
     for (int k = 0; k < N; ++k) {
       int p = k;
       JR amax = fabs(LU(k, k));
@@ -237,6 +275,7 @@ __global__ void __launch_bounds__(TPB, 1) bdf_reactor_kernel(const ReactParams P
       if (p != k)
         for (int j = k; j < N; ++j) { const JR tmp = LU(k, j); LU(k, j) = LU(p, j); LU(p, j) = tmp; }
       const JR inv = JR(1) / LU(k, k);
+      LU(k, k) = inv;
       for (int i = k + 1; i < N; ++i) {
         const JR l = LU(i, k) * inv;
         LU(i, k) = l;
@@ -246,39 +285,30 @@ __global__ void __launch_bounds__(TPB, 1) bdf_reactor_kernel(const ReactParams P
     ++nje;
     gammap = gamma;
     gamrat = 1.0;
-    crate = 1.0;
+    crate2 = 1.0;
     nstlp = nst;
     return ok;
   };
+  // (I - gamma J) x = b with the factors above; the vector lives in shared memory so the
+  // row interchanges are plain indexed accesses
   auto lu_solve = [&](double* b) {
-    JR x[N];
 #pragma unroll
-    for (int i = 0; i < N; ++i) x[i] = (JR)b[i];
+    for (int i = 0; i < N; ++i) XS(i) = (JR)b[i];
+#pragma unroll 1
     for (int k = 0; k < N; ++k) {
       const int p = PIV(k);
-      JR bk = x[k];
-      // permutation applied through a register array needs a dynamic index; keep it in
-      // shared-memory-free form with a select sweep
-      JR bp = bk;
-#pragma unroll
-      for (int i = 0; i < N; ++i) bp = (i == p) ? x[i] : bp;
-#pragma unroll
-      for (int i = 0; i < N; ++i) x[i] = (i == p) ? bk : x[i];
-      x[k] = bp;
-#pragma unroll
-      for (int i = 0; i < N; ++i)
-        if (i > k) x[i] -= LU(i, k) * bp;
+      if (p != k) { const JR tmp = XS(k); XS(k) = XS(p); XS(p) = tmp; }
+      const JR bk = XS(k);
+      for (int i = k + 1; i < N; ++i) XS(i) -= LU(i, k) * bk;
     }
-#pragma unroll
+#pragma unroll 1
     for (int k = N - 1; k >= 0; --k) {
-      JR s = x[k];
-#pragma unroll
-      for (int j = 0; j < N; ++j)
-        if (j > k) s -= LU(k, j) * x[j];
-      x[k] = s / LU(k, k);
+      JR sacc = XS(k);
+      for (int j = k + 1; j < N; ++j) sacc -= LU(k, j) * XS(j);
+      XS(k) = sacc * LU(k, k);
     }
 #pragma unroll
-    for (int i = 0; i < N; ++i) b[i] = (double)x[i];
+    for (int i = 0; i < N; ++i) b[i] = (double)XS(i);
   };
   // ---- cell I/O ----
   auto elem = [&](const ArrDev& a, int n) -> double& {
@@ -364,8 +394,8 @@ __global__ void __launch_bounds__(TPB, 1) bdf_reactor_kernel(const ReactParams P
       for (int i = 0; i < N; ++i) Z(j, i) = 0.0;
     for (int j = 0; j <= QMAX + 1; ++j) TAU(j) = 0.0;
     t = 0.0; h = 0.0; hscale = 0.0; etamax = ETAMX1; eta = 1.0;
-    gamma = 0.0; gammap = 0.0; gamrat = 1.0; crate = 1.0; rl1 = 1.0;
-    tq1 = tq2 = tq3 = tq4 = tq5 = tq5_saved = 1.0;
+    gamma = 0.0; gammap = 0.0; gamrat = 1.0; crate2 = 1.0; rl1 = 1.0;
+    tq1 = tq2 = tq3 = tq5 = tq5_saved = inv_tq4_sq = 1.0;
     q = 1; qwait = 2; nef = 0; ncf = 0; m = 0; status = OK;
     nst = 0; nfe = 0; nje = 0; nstlp = 0; netf = 0; ncfn = 0;
     new_step = true; need_setup = true; force_setup = true; jcur = false;
@@ -468,7 +498,7 @@ __global__ void __launch_bounds__(TPB, 1) bdf_reactor_kernel(const ReactParams P
       double d[N];
 #pragma unroll
       for (int i = 0; i < N; ++i) d[i] = (f[i] - Z(1, i)) / hg;
-      const double ydd = wrms(d);
+      const double ydd = sqrt(wms(d));
       double hnew = (ydd * hub * hub > 2.0) ? sqrt(2.0 / ydd) : sqrt(hg * hub);
       bool done = false;
       if (hin_count == 4) {
@@ -511,17 +541,18 @@ __global__ void __launch_bounds__(TPB, 1) bdf_reactor_kernel(const ReactParams P
 #pragma unroll
           for (int i = 0; i < N; ++i) b[i] *= s;
         }
-        del = wrms(b);
+        del2 = wms(b);
 #pragma unroll
         for (int i = 0; i < N; ++i) { acor[i] += b[i]; y[i] = Z(0, i) + acor[i]; }
-        if (m > 0) crate = fmax(CRDOWN * crate, del / delp);
-        const double dcon = del * fmin(1.0, crate) / tq4;
-        if (dcon <= 1.0) {
+        if (m > 0) crate2 = fmax((CRDOWN * CRDOWN) * crate2, del2 / delp2);
+        // convergence: del * min(1, crate) / tq4 <= 1, in squares
+        const double dcon2 = del2 * fmin(1.0, crate2) * inv_tq4_sq;
+        if (dcon2 <= 1.0) {
           outcome = 1;
         } else {
           ++m;
-          if (m == MAXCOR || (m >= 2 && del > RDIV * delp)) outcome = 2;
-          else delp = del;
+          if (m == MAXCOR || (m >= 2 && del2 > (RDIV * RDIV) * delp2)) outcome = 2;
+          else delp2 = del2;
         }
       }
       if (outcome == 2 && !jcur) {
@@ -542,18 +573,18 @@ __global__ void __launch_bounds__(TPB, 1) bdf_reactor_kernel(const ReactParams P
           phase = STEP;
         }
       } else if (outcome == 1) {
-        const double acnrm = (m == 0) ? del : wrms(acor);
-        const double dsm = acnrm * tq2;
-        if (!(dsm <= 1.0)) {
+        const double acnrm2 = (m == 0) ? del2 : wms(acor);
+        const double dsm2 = acnrm2 * (tq2 * tq2);  // squared local error estimate
+        if (!(dsm2 <= 1.0)) {
           // ---- local error test failed ----
           retract();
           ++nef; ++netf;
-          if (nef >= MXNEF || !isfinite(dsm)) {
-            fail_cell(isfinite(dsm) ? ERRTEST : NONFINITE);
+          if (nef >= MXNEF || !isfinite(dsm2)) {
+            fail_cell(isfinite(dsm2) ? ERRTEST : NONFINITE);
           } else {
             etamax = 1.0;
             if (nef <= MXNEF1) {
-              double e = 1.0 / (pow(BIAS2 * dsm, 1.0 / (q + 1)) + ADDON);
+              double e = 1.0 / (pgb_pow64((BIAS2 * BIAS2) * dsm2, 0.5 * inv_int(q + 1)) + ADDON);
               e = fmax(ETAMIN, e);
               if (nef >= SMALL_NEF) e = fmin(e, ETAMXF);
               rescale(e);
@@ -591,7 +622,7 @@ __global__ void __launch_bounds__(TPB, 1) bdf_reactor_kernel(const ReactParams P
             finish_cell();
           } else {
             // ---- next step size and order ----
-            const double etaq = 1.0 / (pow(BIAS2 * dsm, 1.0 / (q + 1)) + ADDON);
+            const double etaq = 1.0 / (pgb_pow64((BIAS2 * BIAS2) * dsm2, 0.5 * inv_int(q + 1)) + ADDON);
             int qprime = q;
             if (etamax == 1.0) {
               qwait = max(qwait, 2);
@@ -605,16 +636,19 @@ __global__ void __launch_bounds__(TPB, 1) bdf_reactor_kernel(const ReactParams P
                   double zq[N];
 #pragma unroll
                   for (int i = 0; i < N; ++i) zq[i] = Z(q, i);
-                  const double ddn = wrms(zq) * tq1;
-                  etaqm1 = 1.0 / (pow(BIAS1 * ddn, 1.0 / q) + ADDON);
+                  const double ddn2 = wms(zq) * (tq1 * tq1);
+                  etaqm1 = 1.0 / (pgb_pow64((BIAS1 * BIAS1) * ddn2, 0.5 * inv_int(q)) + ADDON);
                 }
                 if (q != qmax) {
-                  const double cquot = (tq5 / tq5_saved) * pow(h / TAU(2), (double)(q + 1));
+                  const double hr = h / TAU(2);
+                  double hrp = hr;
+                  for (int k = 0; k < q; ++k) hrp *= hr;  // (h / tau2)^(q+1)
+                  const double cquot = (tq5 / tq5_saved) * hrp;
                   double tv[N];
 #pragma unroll
                   for (int i = 0; i < N; ++i) tv[i] = acor[i] - cquot * Z(QMAX + 1, i);
-                  const double dup = wrms(tv) * tq3;
-                  etaqp1 = 1.0 / (pow(BIAS3 * dup, 1.0 / (q + 2)) + ADDON);
+                  const double dup2 = wms(tv) * (tq3 * tq3);
+                  etaqp1 = 1.0 / (pgb_pow64((BIAS3 * BIAS3) * dup2, 0.5 * inv_int(q + 2)) + ADDON);
                 }
                 const double etam = fmax(etaqm1, fmax(etaq, etaqp1));
                 if (etam < THRESH) {
@@ -656,6 +690,7 @@ __global__ void __launch_bounds__(TPB, 1) bdf_reactor_kernel(const ReactParams P
 #undef FRC
 #undef LU
 #undef PIV
+#undef XS
 }
 
 }  // namespace pgb

@@ -1,4 +1,6 @@
-// Table-driven FP64 exponential (method of Tang, ACM TOMS 15(2) 1989, 64-entry variant).
+// Table-driven FP64 exponential and logarithm.
+//
+// Exponential: method of Tang, ACM TOMS 15(2) 1989, 64-entry variant.
 //
 //   x = N ln2/64 + r,  N = round(x 64/ln2),  |r| <= ln2/128
 //   exp(x) = 2^(N>>6) * T[N&63] * (1 + p(r)),  T[j] = 2^(j/64),
@@ -39,6 +41,32 @@ __device__ __forceinline__ double pgb_exp64(double x) {
   res = (m > 1023) ? __longlong_as_double(0x7ff0000000000000LL) : res;
   return res;
 }
+
+// Logarithm: method of Tang, ACM TOMS 16(4) 1990, 64 breakpoints c_j = 1 + (j + 1/2)/64:
+//   x = 2^e m (m in [1, 2)),  j = top six mantissa bits,  r = m / c_j - 1 in (-1/128, 1/128)
+//   log x = e ln2 + log c_j + log1p(r),  log1p(r) = r - r^2/2 + ... + r^7/7 (truncation < 2e-17).
+// Eleven FP64 pipe instructions (r through one FMA with a tabulated 1/c_j; the exponent and
+// table index come from integer ops). Defined for positive normal x, the only arguments the
+// rate code passes (temperatures, clipped reduced pressures, Troe centring factors).
+__device__ __constant__ static const double kLog64InvC[64] = PGB_LOG64_INVC;
+__device__ __constant__ static const double kLog64LogC[64] = PGB_LOG64_LOGC;
+
+__device__ __forceinline__ double pgb_log64(double x) {
+  const int hi = __double2hiint(x);
+  const int lo = __double2loint(x);
+  const int e = ((hi >> 20) & 0x7ff) - 1023;
+  const int j = (hi >> 14) & 63;
+  const double m = __hiloint2double((hi & 0x000fffff) | 0x3ff00000, lo);
+  const double r = fma(m, kLog64InvC[j], -1.0);
+  const double r2 = r * r;
+  double p = fma(r, fma(r, fma(r, fma(r, fma(r, 1.0 / 7.0, -1.0 / 6.0), 0.2), -0.25), 1.0 / 3.0), -0.5);
+  p = fma(r2, p, r);
+  const double ed = (double)e;
+  return fma(ed, PGB_LOG64_LN2_HI, kLog64LogC[j] + fma(ed, PGB_LOG64_LN2_LO, p));
+}
+
+// x^a for x > 0 through the two functions above (step-size heuristics).
+__device__ __forceinline__ double pgb_pow64(double x, double a) { return pgb_exp64(a * pgb_log64(x)); }
 
 }  // namespace pgb
 

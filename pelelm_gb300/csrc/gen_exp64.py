@@ -1,8 +1,11 @@
-"""Generates exp64_table.cuh: constants of the table-driven FP64 exponential.
+"""Generates exp64_table.cuh: constants of the table-driven FP64 exponential and logarithm.
 
-Method: Tang, "Table-driven implementation of the exponential function in IEEE
-floating-point arithmetic", ACM TOMS 15(2), 1989 — here with 64 table entries:
+exp: Tang, "Table-driven implementation of the exponential function in IEEE floating-point
+arithmetic", ACM TOMS 15(2), 1989 — here with 64 table entries:
 x = (64 m + j) ln2/64 + r, |r| <= ln2/128, exp(x) = 2^m * 2^(j/64) * exp(r).
+log: Tang, "Table-driven implementation of the logarithm function in IEEE floating-point
+arithmetic", ACM TOMS 16(4), 1990 — 64 breakpoints c_j = 1 + (j + 1/2)/64 on [1, 2):
+x = 2^e m, log x = e ln2 + log c_j + log1p(m/c_j - 1), |m/c_j - 1| < 1/128.
 The constants are computed from their mathematical definitions with mpmath.
 """
 import os
@@ -33,6 +36,15 @@ def main(path):
         f.write(f"#define PGB_EXP64_L1 {L1!r}\n")
         f.write(f"#define PGB_EXP64_L2 {L2!r}\n")
         f.write("#define PGB_EXP64_TABLE {" + ", ".join(repr(t) for t in tab) + "}\n")
+        cj = [1 + (mp.mpf(j) + mp.mpf(1) / 2) / 64 for j in range(64)]
+        f.write("#define PGB_LOG64_INVC {" + ", ".join(repr(float(1 / c)) for c in cj) + "}\n")
+        f.write("#define PGB_LOG64_LOGC {" + ", ".join(repr(float(mp.log(c))) for c in cj) + "}\n")
+        ln2 = mp.log(2)
+        ln2_hi = float(ln2)
+        b = struct.unpack("<Q", struct.pack("<d", ln2_hi))[0] & ~((1 << 21) - 1)
+        ln2_hi = struct.unpack("<d", struct.pack("<Q", b))[0]
+        f.write(f"#define PGB_LOG64_LN2_HI {ln2_hi!r}\n")
+        f.write(f"#define PGB_LOG64_LN2_LO {float(ln2 - mp.mpf(ln2_hi))!r}\n")
 
 
 if __name__ == "__main__":

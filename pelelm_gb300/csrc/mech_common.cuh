@@ -11,7 +11,7 @@ namespace pgb {
 
 // FP64 exponential / logarithm used by every rate evaluation.
 __device__ __forceinline__ double pgb_exp(double x) { return pgb_exp64(x); }
-__device__ __forceinline__ double pgb_log(double x) { return log(x); }
+__device__ __forceinline__ double pgb_log(double x) { return pgb_log64(x); }
 
 // Precision-generic versions used by the Jacobian template. The FP32 path uses the
 // hardware exponential / logarithm with the argument clamped to the finite FP32 range, so

@@ -54,6 +54,7 @@ struct Options {
   bool mixed = true;       // gb.precision = mixed (FP32 J/LU) | fp64
   int tpb = 0;             // 0 = default per mechanism
   bool graph = false;
+  bool lu_global = false;  // gb.lu = shared (default) | global (L2-resident scratch)
   std::string solve_type = "denseAJ_direct";
   int analytical_jacobian = 1;
 };
@@ -83,6 +84,11 @@ int parse_options(const char* s, Options& o) {
         else return set_err("gb.precision must be mixed or fp64, got '%s'", v.c_str());
       } else if (k == "gb.tpb") o.tpb = std::stoi(v);
       else if (k == "gb.graph") o.graph = std::stoi(v) != 0;
+      else if (k == "gb.lu") {
+        if (v == "global") o.lu_global = true;
+        else if (v == "shared") o.lu_global = false;
+        else return set_err("gb.lu must be global or shared, got '%s'", v.c_str());
+      }
       else return set_err("unknown option '%s'", k.c_str());
     } catch (...) {
       return set_err("bad value for option '%s': '%s'", k.c_str(), v.c_str());
@@ -143,6 +149,8 @@ struct Scratch {
   size_t box_cap = 0;
   pgb::BoxDev* h_boxes = nullptr;  // pinned staging
   unsigned long long* d_counter = nullptr;
+  void* d_lu = nullptr;            // Jacobian/LU slices of the resident threads
+  size_t lu_cap = 0;
   pgb::ReactStats* d_stats = nullptr;
   cudaEvent_t done = nullptr;
   long long last_ncell = 0;
@@ -174,6 +182,7 @@ void free_scratch(Scratch& s) {
   if (s.h_boxes) cudaFreeHost(s.h_boxes);
   if (s.d_counter) cudaFree(s.d_counter);
   if (s.d_stats) cudaFree(s.d_stats);
+  if (s.d_lu) cudaFree(s.d_lu);
   if (s.done) cudaEventDestroy(s.done);
   s = Scratch();
 }
@@ -203,11 +212,42 @@ bool same_boxes(const std::vector<pgb::BoxDev>& a, const pgb::BoxDev* b, size_t 
   return a.size() == n && std::memcmp(a.data(), b, n * sizeof(pgb::BoxDev)) == 0;
 }
 
-int default_tpb(const pgb_reactor* r) {
-  const int per = r->opt.mixed ? r->mech->smem_mixed : r->mech->smem_fp64;
-  const int limit = 227 * 1024;
-  if (per * 128 <= limit) return 128;
-  return 64;
+// Threads per block and grid of the persistent launch, and the global Jacobian/LU scratch it
+// needs (0 when the slices live in shared memory).
+struct LaunchPlan {
+  int tpb = 128, nblocks = 1;
+  size_t lu_bytes = 0;
+};
+
+LaunchPlan plan_launch(const pgb_reactor* r, long long ncell) {
+  LaunchPlan pl;
+  const bool g = r->opt.lu_global;
+  const int per = r->opt.mixed ? (g ? r->mech->smem_mixed_g : r->mech->smem_mixed)
+                               : (g ? r->mech->smem_fp64_g : r->mech->smem_fp64);
+  if (r->opt.tpb > 0) pl.tpb = r->opt.tpb;
+  else if (g) pl.tpb = (per * 256 <= kMaxSmemPerBlock) ? 256 : 128;
+  else pl.tpb = (per * 128 <= kMaxSmemPerBlock) ? 128 : 64;
+  // persistent grid: one CTA per SM (the shared-memory footprint admits one), never more
+  // CTAs than there are blocks' worth of cells
+  const long long max_blocks = std::max<long long>(1, (ncell + pl.tpb - 1) / pl.tpb);
+  pl.nblocks = (int)std::min<long long>(r->nsm, max_blocks);
+  if (g) {
+    const int N = r->mech->ns + 1;
+    pl.lu_bytes = (size_t)pl.nblocks * pl.tpb * N * N * (r->opt.mixed ? sizeof(float) : sizeof(double));
+  }
+  return pl;
+}
+
+int ensure_lu(Scratch& s, size_t bytes) {
+  if (bytes <= s.lu_cap) return 0;
+  if (s.done) PGB_CUDA(cudaEventSynchronize(s.done));
+  if (s.gexec) { cudaGraphExecDestroy(s.gexec); s.gexec = nullptr; s.gkey.clear(); }
+  if (s.d_lu) PGB_CUDA(cudaFree(s.d_lu));
+  s.d_lu = nullptr;
+  s.lu_cap = 0;
+  PGB_CUDA(cudaMalloc(&s.d_lu, bytes));
+  s.lu_cap = bytes;
+  return 0;
 }
 
 int enqueue_advance(pgb_reactor* r, Scratch& s, int nbox, long long ncell, double dt,
@@ -234,13 +274,10 @@ int enqueue_advance(pgb_reactor* r, Scratch& s, int nbox, long long ncell, doubl
     const long long nb = std::min<long long>((ncell + 255) / 256, (long long)r->nsm * 8);
     return r->mech->null_fn(p, st, (int)nb);
   }
-  const int tpb = r->opt.tpb > 0 ? r->opt.tpb : default_tpb(r);
-  // persistent grid: one CTA per SM (the shared-memory footprint admits one), never more
-  // CTAs than there are warps' worth of cells
-  const long long max_blocks = std::max<long long>(1, (ncell + tpb - 1) / tpb);
-  const int nblocks = (int)std::min<long long>(r->nsm, max_blocks);
+  const LaunchPlan pl = plan_launch(r, ncell);
+  p.lu_scratch = pl.lu_bytes ? s.d_lu : nullptr;
   LaunchFn fn = r->opt.mixed ? r->mech->bdf_mixed : r->mech->bdf_fp64;
-  return fn(p, tpb, st, nblocks);
+  return fn(p, pl.tpb, st, pl.nblocks);
 }
 
 }  // namespace
@@ -328,6 +365,7 @@ int pgb_reactor_react_boxes(pgb_reactor* r, const pgb_box_view* views, int nbox,
   std::vector<pgb::BoxDev> boxes;
   long long ncell = 0;
   if (build_boxes(views, nbox, r->mech->ns, boxes, ncell)) return -1;
+  if (!r->null_reactor && ensure_lu(*s, plan_launch(r, ncell).lu_bytes)) return -1;
   PGB_CUDA(cudaEventSynchronize(s->done));  // staging buffer may still feed a previous copy
   if (nbox) std::memcpy(s->h_boxes, boxes.data(), nbox * sizeof(pgb::BoxDev));
   s->last_ncell = ncell;

@@ -26,14 +26,14 @@ using LaunchFn = int (*)(const pgb::ReactParams&, int tpb, cudaStream_t, int nbl
 
 constexpr int kMaxSmemPerBlock = 227 * 1024;
 
-template <class M, class JR, int TPB>
+template <class M, class JR, int TPB, bool LU_GLOBAL>
 int launch_bdf_tpb(const pgb::ReactParams& p, cudaStream_t s, int nblocks) {
-  constexpr int smem = pgb::bdf_smem_per_thread<M, JR>() * TPB;
+  constexpr int smem = pgb::bdf_smem_per_thread<M, JR, LU_GLOBAL>() * TPB;
   if constexpr (smem > kMaxSmemPerBlock) {
     return set_err("%s: %d threads per block need %d B of shared memory (limit %d)", M::NAME, TPB,
                    smem, kMaxSmemPerBlock);
   } else {
-    auto kern = pgb::bdf_reactor_kernel<M, JR, TPB>;
+    auto kern = pgb::bdf_reactor_kernel<M, JR, TPB, LU_GLOBAL>;
     PGB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     kern<<<nblocks, TPB, smem, s>>>(p);
     PGB_CUDA(cudaGetLastError());
@@ -41,11 +41,20 @@ int launch_bdf_tpb(const pgb::ReactParams& p, cudaStream_t s, int nblocks) {
   }
 }
 
+// Launches the persistent BDF kernel with `tpb` threads per block; the Jacobian/LU slices go to
+// p.lu_scratch when it is set (sized for nblocks * tpb threads), else to shared memory.
 template <class M, class JR>
 int launch_bdf(const pgb::ReactParams& p, int tpb, cudaStream_t s, int nblocks) {
+  if (p.lu_scratch) {
+    switch (tpb) {
+      case 128: return launch_bdf_tpb<M, JR, 128, true>(p, s, nblocks);
+      case 256: return launch_bdf_tpb<M, JR, 256, true>(p, s, nblocks);
+      default: return set_err("gb.tpb=%d is not compiled (128, 256)", tpb);
+    }
+  }
   switch (tpb) {
-    case 64: return launch_bdf_tpb<M, JR, 64>(p, s, nblocks);
-    case 128: return launch_bdf_tpb<M, JR, 128>(p, s, nblocks);
+    case 64: return launch_bdf_tpb<M, JR, 64, false>(p, s, nblocks);
+    case 128: return launch_bdf_tpb<M, JR, 128, false>(p, s, nblocks);
     default: return set_err("gb.tpb=%d is not compiled (64, 128)", tpb);
   }
 }
@@ -62,7 +71,8 @@ struct MechEntry {
   int ns, nr;
   LaunchFn bdf_mixed, bdf_fp64;
   int (*null_fn)(const pgb::ReactParams&, cudaStream_t, int);
-  int smem_mixed, smem_fp64;  // bytes per thread
+  int smem_mixed, smem_fp64;  // shared bytes per thread, LU in shared memory
+  int smem_mixed_g, smem_fp64_g;  // shared bytes per thread, LU in global scratch
   int (*rates_fn)(const pgb_box_view*, const pgb_array4*, cudaStream_t);
   int (*h2t_fn)(const pgb_box_view*, double, double, cudaStream_t);
 };
@@ -134,7 +144,8 @@ int h2t_entry(const pgb_box_view* v, double tmin, double tmax, cudaStream_t s) {
   ::pgb_host::MechEntry {                                                                    \
     M::NAME, M::NS, M::NR, ::pgb_host::launch_bdf<M, float>, ::pgb_host::launch_bdf<M, double>, \
         ::pgb_host::launch_null<M>, pgb::bdf_smem_per_thread<M, float>(),                    \
-        pgb::bdf_smem_per_thread<M, double>(), ::pgb_host::rates_entry<M>,                   \
+        pgb::bdf_smem_per_thread<M, double>(), pgb::bdf_smem_per_thread<M, float, true>(),   \
+        pgb::bdf_smem_per_thread<M, double, true>(), ::pgb_host::rates_entry<M>,             \
         ::pgb_host::h2t_entry<M>                                                             \
   }
 

@@ -51,6 +51,7 @@ struct ReactParams {
   int max_steps;
   unsigned long long* next_cell;  // work queue head (device scratch)
   ReactStats* stats;              // device scratch
+  void* lu_scratch;               // per-thread Jacobian/LU slices in global memory, or null
 };
 
 }  // namespace pgb

