@@ -62,7 +62,8 @@ typedef struct {
  * (pgb_mechanism_info). reactor_type must be 2 (rho h, constant pressure), the value PeleLM uses.
  * options: whitespace/semicolon separated key=value pairs — the reference's runtime keys
  * ode.rtol, ode.atol, cvode.max_order, cvode.solve_type, ode.analytical_jacobian,
- * peleLM.use_typ_vals_chem, plus ode.max_steps, gb.precision=fp64|mixed, gb.tpb, gb.graph=0|1.
+ * peleLM.use_typ_vals_chem, plus ode.max_steps, gb.precision=fp64|mixed, gb.tpb, gb.graph=0|1,
+ * gb.history=shared|global.
  * Returns NULL on error. */
 pgb_reactor* pgb_reactor_create(const char* name, const char* mechanism, int reactor_type,
                                 const char* options);

@@ -35,6 +35,7 @@ def generate_sources() -> None:
     from .mech import codegen
     gen = os.path.join(CSRC, "gen")
     codegen.main(gen, names=("lidryer_syn", "drm19_syn"))
+    codegen.write_tables(gen, names=("lidryer_syn", "drm19_syn"))
     # the exp64 constants are committed (their generator needs mpmath, absent on some hosts)
     if not os.path.exists(os.path.join(gen, "exp64_table.cuh")):
         subprocess.check_call([sys.executable, os.path.join(CSRC, "gen_exp64.py")])

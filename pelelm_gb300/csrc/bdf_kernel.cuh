@@ -26,6 +26,7 @@
 #include <float.h>
 
 #include "mech_common.cuh"
+#include "mech_tables.cuh"
 #include "reactor_types.cuh"
 
 namespace pgb {
@@ -57,17 +58,22 @@ __device__ __forceinline__ double recip_fast(double x) {
 enum Status : int { OK = 0, MAX_STEPS = 1, ERRTEST = 2, CONV = 3, HSMALL = 4, NONFINITE = 5 };
 }  // namespace bdf
 
-// Bytes of dynamic shared memory per thread for mechanism M with Jacobian type JR; the
-// Jacobian/LU slice lives in shared memory unless LU_GLOBAL (then in the L2-resident global
-// scratch ReactParams::lu_scratch, one [N*N][slot] array over all resident threads).
-template <class M, class JR, bool LU_GLOBAL = false>
+// Where the per-thread arrays live: shared memory by default; LAYOUT_LU_GLOBAL puts the
+// Jacobian/LU slice and LAYOUT_Z_GLOBAL the Nordsieck history into L2-resident global scratch
+// (ReactParams::lu_scratch / z_scratch, each an [element][slot] array over all resident
+// threads, so a warp's access to one element is one contiguous 256 B line).
+enum : int { LAYOUT_LU_GLOBAL = 1, LAYOUT_Z_GLOBAL = 2 };
+
+// Bytes of dynamic shared memory per thread for mechanism M, Jacobian type JR and LAYOUT.
+template <class M, class JR, int LAYOUT = 0>
 __host__ __device__ constexpr int bdf_smem_per_thread() {
-  return (QMAX + 2) * M::N * 8    // Nordsieck z[0..QMAX] + saved correction
+  return ((LAYOUT & LAYOUT_Z_GLOBAL) ? 0 : (QMAX + 2) * M::N * 8)  // Nordsieck + saved correction
          + (QMAX + 1) * 8         // l coefficients
          + (QMAX + 2) * 8         // step history tau
          + M::N * 8               // forcing (F_rhoY, F_rhoh)
          + M::N * (int)sizeof(JR)  // triangular-solve vector
-         + (LU_GLOBAL ? 0 : M::N * M::N * (int)sizeof(JR))  // Jacobian / LU
+         + ((LAYOUT & LAYOUT_LU_GLOBAL) ? 0 : M::N * M::N * (int)sizeof(JR))  // Jacobian / LU
+         + (M::RHS_TABLE ? 3 * M::NS * 8 : 0)  // table RHS: concentrations, g/RT, production
          + ((M::N + 7) / 8) * 8;  // pivots
 }
 
@@ -81,8 +87,10 @@ struct LuAcc {  // J(i,k) view of one thread's matrix slice, element stride `str
   }
 };
 
-template <class M, class JR, int TPB, bool LU_GLOBAL = false>
+template <class M, class JR, int TPB, int LAYOUT = 0>
 __global__ void __launch_bounds__(TPB, 1) bdf_reactor_kernel(const ReactParams P) {
+  constexpr bool LU_GLOBAL = (LAYOUT & LAYOUT_LU_GLOBAL) != 0;
+  constexpr bool Z_GLOBAL = (LAYOUT & LAYOUT_Z_GLOBAL) != 0;
   using namespace bdf;
   constexpr bool MIXED = sizeof(JR) == sizeof(float);
   constexpr int N = M::N;
@@ -90,19 +98,23 @@ __global__ void __launch_bounds__(TPB, 1) bdf_reactor_kernel(const ReactParams P
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int tid = threadIdx.x;
   const int lane = tid & 31;
-  double* Zs = reinterpret_cast<double*>(smem_raw);            // [(QMAX+2)*N][TPB]
-  double* Ls = Zs + (QMAX + 2) * N * TPB;                      // [QMAX+1][TPB]
-  double* TAUs = Ls + (QMAX + 1) * TPB;                        // [QMAX+2][TPB]
-  double* Fs = TAUs + (QMAX + 2) * TPB;                        // [N][TPB]
-  JR* XSs = reinterpret_cast<JR*>(Fs + N * TPB);               // [N][TPB] solve vector
-  JR* LUs = XSs + N * TPB;                                      // [N*N][TPB] (shared variant)
-  unsigned char* PIVs =
-      reinterpret_cast<unsigned char*>(LU_GLOBAL ? reinterpret_cast<JR*>(LUs) : LUs + N * N * TPB);  // [N][TPB]
-  // this thread's Jacobian / LU slice and its element stride
-  JR* const LUb = LU_GLOBAL ? static_cast<JR*>(P.lu_scratch) + (long long)blockIdx.x * TPB + tid
-                            : LUs + tid;
-  const long long lu_stride = LU_GLOBAL ? (long long)gridDim.x * TPB : (long long)TPB;
-#define Z(j, i) Zs[((j) * N + (i)) * TPB + tid]
+  double* const smem_d = reinterpret_cast<double*>(smem_raw);
+  double* Zs = smem_d;                                           // [(QMAX+2)*N][TPB] unless global
+  double* Ls = Z_GLOBAL ? smem_d : Zs + (QMAX + 2) * N * TPB;    // [QMAX+1][TPB]
+  double* TAUs = Ls + (QMAX + 1) * TPB;                          // [QMAX+2][TPB]
+  double* Fs = TAUs + (QMAX + 2) * TPB;                          // [N][TPB]
+  JR* XSs = reinterpret_cast<JR*>(Fs + N * TPB);                 // [N][TPB] solve vector
+  JR* LUs = XSs + N * TPB;                                       // [N*N][TPB] unless global
+  double* RSs = reinterpret_cast<double*>(LU_GLOBAL ? LUs : LUs + N * N * TPB);  // [3*NS][TPB] table RHS
+  unsigned char* PIVs = reinterpret_cast<unsigned char*>(RSs + (M::RHS_TABLE ? 3 * NS * TPB : 0));
+  const long long slot = (long long)blockIdx.x * TPB + tid;
+  const long long nslot = (long long)gridDim.x * TPB;
+  // this thread's Jacobian / LU slice and Nordsieck slice, with their element strides
+  JR* const LUb = LU_GLOBAL ? static_cast<JR*>(P.lu_scratch) + slot : LUs + tid;
+  const long long lu_stride = LU_GLOBAL ? nslot : (long long)TPB;
+  double* const Zb = Z_GLOBAL ? static_cast<double*>(P.z_scratch) + slot : Zs + tid;
+  const long long z_stride = Z_GLOBAL ? nslot : (long long)TPB;
+#define Z(j, i) Zb[(long long)((j) * N + (i)) * z_stride]
 #define LCO(j) Ls[(j) * TPB + tid]
 #define TAU(j) TAUs[(j) * TPB + tid]
 #define FRC(i) Fs[(i) * TPB + tid]
@@ -252,10 +264,16 @@ __global__ void __launch_bounds__(TPB, 1) bdf_reactor_kernel(const ReactParams P
   // M = I - gamma J in the LU slice, factor with partial pivoting (trailing swaps)
   auto setup_matrix = [&]() -> bool {
     LuAcc<JR> acc{LUb, N, lu_stride};
-    double Fl[NS];
+    if constexpr (M::JAC_TABLE) {
+      // concentrations go to the solve vector (free during the setup); forcing read in place
+      jac_table<typename M::Tab, JR>(y, [&](int k) -> double { return FRC(k); }, FRC(NS), acc,
+                                     [&](int k) -> JR& { return XS(k); });
+    } else {
+      double Fl[NS];
 #pragma unroll
-    for (int i = 0; i < NS; ++i) Fl[i] = FRC(i);
-    M::template jac<JR>(y, Fl, FRC(NS), acc);
+      for (int i = 0; i < NS; ++i) Fl[i] = FRC(i);
+      M::template jac<JR>(y, Fl, FRC(NS), acc);
+    }
     const JR g = (JR)gamma;
 #pragma unroll 1
     for (int i = 0; i < N; ++i)
@@ -461,10 +479,17 @@ __global__ void __launch_bounds__(TPB, 1) bdf_reactor_kernel(const ReactParams P
     double f[N];
     const bool active = phase >= START;
     if (active) {
-      double Fl[NS];
+      if constexpr (M::RHS_TABLE) {
+        rhs_table<typename M::Tab>(y, [&](int k) -> double { return FRC(k); }, FRC(NS), f,
+                                   [&](int k) -> double& { return RSs[k * TPB + tid]; },
+                                   [&](int k) -> double& { return RSs[(NS + k) * TPB + tid]; },
+                                   [&](int k) -> double& { return RSs[(2 * NS + k) * TPB + tid]; });
+      } else {
+        double Fl[NS];
 #pragma unroll
-      for (int i = 0; i < NS; ++i) Fl[i] = FRC(i);
-      M::rhs(y, Fl, FRC(NS), f);
+        for (int i = 0; i < NS; ++i) Fl[i] = FRC(i);
+        M::rhs(y, Fl, FRC(NS), f);
+      }
       ++nfe;
     }
 

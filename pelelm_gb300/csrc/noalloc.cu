@@ -99,7 +99,8 @@ extern "C" int pgb_react_boxes_noalloc(const char* mechanism, const pgb_box_view
   p.max_steps = max_steps;
   p.next_cell = &S->next_cell;
   p.stats = &S->stats;
-  p.lu_scratch = nullptr;  // Jacobian/LU slices stay in shared memory
+  p.lu_scratch = nullptr;  // Jacobian/LU slices and Nordsieck histories stay in shared memory
+  p.z_scratch = nullptr;
   int dev = 0, nsm = 0;
   PGB_CUDA(cudaGetDevice(&dev));
   PGB_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));

@@ -54,7 +54,8 @@ struct Options {
   bool mixed = true;       // gb.precision = mixed (FP32 J/LU) | fp64
   int tpb = 0;             // 0 = default per mechanism
   bool graph = false;
-  bool lu_global = false;  // gb.lu = shared (default) | global (L2-resident scratch)
+  int z_global = -1;       // gb.history = shared | global (L2-resident Nordsieck); -1 = auto
+  int lu_global = -1;      // gb.lu = shared | global (L2-resident Jacobian/LU); -1 = auto
   std::string solve_type = "denseAJ_direct";
   int analytical_jacobian = 1;
 };
@@ -84,10 +85,11 @@ int parse_options(const char* s, Options& o) {
         else return set_err("gb.precision must be mixed or fp64, got '%s'", v.c_str());
       } else if (k == "gb.tpb") o.tpb = std::stoi(v);
       else if (k == "gb.graph") o.graph = std::stoi(v) != 0;
-      else if (k == "gb.lu") {
-        if (v == "global") o.lu_global = true;
-        else if (v == "shared") o.lu_global = false;
-        else return set_err("gb.lu must be global or shared, got '%s'", v.c_str());
+      else if (k == "gb.history" || k == "gb.lu") {
+        int& f = (k == "gb.history") ? o.z_global : o.lu_global;
+        if (v == "global") f = 1;
+        else if (v == "shared") f = 0;
+        else return set_err("%s must be global or shared, got '%s'", k.c_str(), v.c_str());
       }
       else return set_err("unknown option '%s'", k.c_str());
     } catch (...) {
@@ -149,6 +151,8 @@ struct Scratch {
   size_t box_cap = 0;
   pgb::BoxDev* h_boxes = nullptr;  // pinned staging
   unsigned long long* d_counter = nullptr;
+  void* d_z = nullptr;             // Nordsieck histories of the resident threads
+  size_t z_cap = 0;
   void* d_lu = nullptr;            // Jacobian/LU slices of the resident threads
   size_t lu_cap = 0;
   pgb::ReactStats* d_stats = nullptr;
@@ -182,6 +186,7 @@ void free_scratch(Scratch& s) {
   if (s.h_boxes) cudaFreeHost(s.h_boxes);
   if (s.d_counter) cudaFree(s.d_counter);
   if (s.d_stats) cudaFree(s.d_stats);
+  if (s.d_z) cudaFree(s.d_z);
   if (s.d_lu) cudaFree(s.d_lu);
   if (s.done) cudaEventDestroy(s.done);
   s = Scratch();
@@ -212,41 +217,55 @@ bool same_boxes(const std::vector<pgb::BoxDev>& a, const pgb::BoxDev* b, size_t 
   return a.size() == n && std::memcmp(a.data(), b, n * sizeof(pgb::BoxDev)) == 0;
 }
 
-// Threads per block and grid of the persistent launch, and the global Jacobian/LU scratch it
-// needs (0 when the slices live in shared memory).
+// Threads per block and grid of the persistent launch, and the global Nordsieck scratch it
+// needs (0 when the histories live in shared memory).
 struct LaunchPlan {
   int tpb = 128, nblocks = 1;
-  size_t lu_bytes = 0;
+  bool z_global = false, lu_global = false;
+  size_t z_bytes = 0, lu_bytes = 0;
 };
 
+// First layout (all shared; global Nordsieck history; global history and LU) whose shared
+// footprint fits 128 threads per block (the occupancy that measures best), unless options
+// force the layout or the block size.
 LaunchPlan plan_launch(const pgb_reactor* r, long long ncell) {
   LaunchPlan pl;
-  const bool g = r->opt.lu_global;
-  const int per = r->opt.mixed ? (g ? r->mech->smem_mixed_g : r->mech->smem_mixed)
-                               : (g ? r->mech->smem_fp64_g : r->mech->smem_fp64);
-  if (r->opt.tpb > 0) pl.tpb = r->opt.tpb;
-  else if (g) pl.tpb = (per * 256 <= kMaxSmemPerBlock) ? 256 : 128;
-  else pl.tpb = (per * 128 <= kMaxSmemPerBlock) ? 128 : 64;
-  // persistent grid: one CTA per SM (the shared-memory footprint admits one), never more
-  // CTAs than there are blocks' worth of cells
+  const MechEntry& m = *r->mech;
+  const int per[3] = {r->opt.mixed ? m.smem_mixed : m.smem_fp64, r->opt.mixed ? m.smem_mixed_g : m.smem_fp64_g,
+                      r->opt.mixed ? m.smem_mixed_gl : m.smem_fp64_gl};
+  const int tpb = r->opt.tpb > 0 ? r->opt.tpb : 128;
+  int choice = -1;
+  for (int c = 0; c < 3 && choice < 0; ++c) {
+    const bool zg = c >= 1, lg = c >= 2;
+    if (r->opt.z_global >= 0 && (r->opt.z_global == 1) != zg) continue;
+    if (r->opt.lu_global >= 0 && (r->opt.lu_global == 1) != lg) continue;
+    if (per[c] * tpb <= kMaxSmemPerBlock) choice = c;
+  }
+  if (choice < 0) choice = 2;  // the launch reports the shared-memory shortfall
+  pl.tpb = tpb;
+  pl.z_global = choice >= 1;
+  pl.lu_global = choice >= 2;
+  // persistent grid: one CTA per SM, never more CTAs than there are blocks' worth of cells
   const long long max_blocks = std::max<long long>(1, (ncell + pl.tpb - 1) / pl.tpb);
   pl.nblocks = (int)std::min<long long>(r->nsm, max_blocks);
-  if (g) {
-    const int N = r->mech->ns + 1;
-    pl.lu_bytes = (size_t)pl.nblocks * pl.tpb * N * N * (r->opt.mixed ? sizeof(float) : sizeof(double));
-  }
+  const int N = m.ns + 1;
+  const size_t slots = (size_t)pl.nblocks * pl.tpb;
+  if (pl.z_global) pl.z_bytes = slots * (pgb::QMAX + 2) * N * sizeof(double);
+  if (pl.lu_global) pl.lu_bytes = slots * N * N * (r->opt.mixed ? sizeof(float) : sizeof(double));
   return pl;
 }
 
-int ensure_lu(Scratch& s, size_t bytes) {
-  if (bytes <= s.lu_cap) return 0;
+// Grows one global scratch buffer (outside any stream capture; captured graphs that point at
+// the old buffer are dropped).
+int ensure_buf(Scratch& s, void*& buf, size_t& cap, size_t bytes) {
+  if (bytes <= cap) return 0;
   if (s.done) PGB_CUDA(cudaEventSynchronize(s.done));
   if (s.gexec) { cudaGraphExecDestroy(s.gexec); s.gexec = nullptr; s.gkey.clear(); }
-  if (s.d_lu) PGB_CUDA(cudaFree(s.d_lu));
-  s.d_lu = nullptr;
-  s.lu_cap = 0;
-  PGB_CUDA(cudaMalloc(&s.d_lu, bytes));
-  s.lu_cap = bytes;
+  if (buf) PGB_CUDA(cudaFree(buf));
+  buf = nullptr;
+  cap = 0;
+  PGB_CUDA(cudaMalloc(&buf, bytes));
+  cap = bytes;
   return 0;
 }
 
@@ -276,6 +295,7 @@ int enqueue_advance(pgb_reactor* r, Scratch& s, int nbox, long long ncell, doubl
   }
   const LaunchPlan pl = plan_launch(r, ncell);
   p.lu_scratch = pl.lu_bytes ? s.d_lu : nullptr;
+  p.z_scratch = pl.z_bytes ? s.d_z : nullptr;
   LaunchFn fn = r->opt.mixed ? r->mech->bdf_mixed : r->mech->bdf_fp64;
   return fn(p, pl.tpb, st, pl.nblocks);
 }
@@ -365,7 +385,11 @@ int pgb_reactor_react_boxes(pgb_reactor* r, const pgb_box_view* views, int nbox,
   std::vector<pgb::BoxDev> boxes;
   long long ncell = 0;
   if (build_boxes(views, nbox, r->mech->ns, boxes, ncell)) return -1;
-  if (!r->null_reactor && ensure_lu(*s, plan_launch(r, ncell).lu_bytes)) return -1;
+  if (!r->null_reactor) {
+    const LaunchPlan pl = plan_launch(r, ncell);
+    if (ensure_buf(*s, s->d_z, s->z_cap, pl.z_bytes) || ensure_buf(*s, s->d_lu, s->lu_cap, pl.lu_bytes))
+      return -1;
+  }
   PGB_CUDA(cudaEventSynchronize(s->done));  // staging buffer may still feed a previous copy
   if (nbox) std::memcpy(s->h_boxes, boxes.data(), nbox * sizeof(pgb::BoxDev));
   s->last_ncell = ncell;

@@ -26,14 +26,14 @@ using LaunchFn = int (*)(const pgb::ReactParams&, int tpb, cudaStream_t, int nbl
 
 constexpr int kMaxSmemPerBlock = 227 * 1024;
 
-template <class M, class JR, int TPB, bool LU_GLOBAL>
+template <class M, class JR, int TPB, int LAYOUT>
 int launch_bdf_tpb(const pgb::ReactParams& p, cudaStream_t s, int nblocks) {
-  constexpr int smem = pgb::bdf_smem_per_thread<M, JR, LU_GLOBAL>() * TPB;
+  constexpr int smem = pgb::bdf_smem_per_thread<M, JR, LAYOUT>() * TPB;
   if constexpr (smem > kMaxSmemPerBlock) {
     return set_err("%s: %d threads per block need %d B of shared memory (limit %d)", M::NAME, TPB,
                    smem, kMaxSmemPerBlock);
   } else {
-    auto kern = pgb::bdf_reactor_kernel<M, JR, TPB, LU_GLOBAL>;
+    auto kern = pgb::bdf_reactor_kernel<M, JR, TPB, LAYOUT>;
     PGB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     kern<<<nblocks, TPB, smem, s>>>(p);
     PGB_CUDA(cudaGetLastError());
@@ -41,21 +41,30 @@ int launch_bdf_tpb(const pgb::ReactParams& p, cudaStream_t s, int nblocks) {
   }
 }
 
-// Launches the persistent BDF kernel with `tpb` threads per block; the Jacobian/LU slices go to
-// p.lu_scratch when it is set (sized for nblocks * tpb threads), else to shared memory.
+template <class M, class JR, int LAYOUT>
+int launch_bdf_layout(const pgb::ReactParams& p, int tpb, cudaStream_t s, int nblocks) {
+  // 64 threads only for the all-shared layout (the allocation-free entry's fallback), 256 only
+  // for the global layouts
+  if (tpb == 128) return launch_bdf_tpb<M, JR, 128, LAYOUT>(p, s, nblocks);
+  if constexpr (LAYOUT == 0) {
+    if (tpb == 64) return launch_bdf_tpb<M, JR, 64, LAYOUT>(p, s, nblocks);
+  } else {
+    if (tpb == 256) return launch_bdf_tpb<M, JR, 256, LAYOUT>(p, s, nblocks);
+  }
+  return set_err("gb.tpb=%d is not compiled for this layout (64/128 shared, 128/256 global)", tpb);
+}
+
+// Launches the persistent BDF kernel with `tpb` threads per block; the Jacobian/LU slices and
+// the Nordsieck histories go to p.lu_scratch / p.z_scratch when those are set (sized for
+// nblocks * tpb threads), else to shared memory.
 template <class M, class JR>
 int launch_bdf(const pgb::ReactParams& p, int tpb, cudaStream_t s, int nblocks) {
-  if (p.lu_scratch) {
-    switch (tpb) {
-      case 128: return launch_bdf_tpb<M, JR, 128, true>(p, s, nblocks);
-      case 256: return launch_bdf_tpb<M, JR, 256, true>(p, s, nblocks);
-      default: return set_err("gb.tpb=%d is not compiled (128, 256)", tpb);
-    }
-  }
-  switch (tpb) {
-    case 64: return launch_bdf_tpb<M, JR, 64, false>(p, s, nblocks);
-    case 128: return launch_bdf_tpb<M, JR, 128, false>(p, s, nblocks);
-    default: return set_err("gb.tpb=%d is not compiled (64, 128)", tpb);
+  const int layout = (p.lu_scratch ? pgb::LAYOUT_LU_GLOBAL : 0) | (p.z_scratch ? pgb::LAYOUT_Z_GLOBAL : 0);
+  switch (layout) {
+    case 0: return launch_bdf_layout<M, JR, 0>(p, tpb, s, nblocks);
+    case 2: return launch_bdf_layout<M, JR, 2>(p, tpb, s, nblocks);
+    case 3: return launch_bdf_layout<M, JR, 3>(p, tpb, s, nblocks);
+    default: return set_err("a global Jacobian/LU without a global history is not compiled");
   }
 }
 
@@ -71,8 +80,9 @@ struct MechEntry {
   int ns, nr;
   LaunchFn bdf_mixed, bdf_fp64;
   int (*null_fn)(const pgb::ReactParams&, cudaStream_t, int);
-  int smem_mixed, smem_fp64;  // shared bytes per thread, LU in shared memory
-  int smem_mixed_g, smem_fp64_g;  // shared bytes per thread, LU in global scratch
+  int smem_mixed, smem_fp64;  // shared bytes per thread, everything in shared memory
+  int smem_mixed_g, smem_fp64_g;  // shared bytes per thread, Nordsieck history in global scratch
+  int smem_mixed_gl, smem_fp64_gl;  // shared bytes per thread, history and LU in global scratch
   int (*rates_fn)(const pgb_box_view*, const pgb_array4*, cudaStream_t);
   int (*h2t_fn)(const pgb_box_view*, double, double, cudaStream_t);
 };
@@ -144,8 +154,11 @@ int h2t_entry(const pgb_box_view* v, double tmin, double tmax, cudaStream_t s) {
   ::pgb_host::MechEntry {                                                                    \
     M::NAME, M::NS, M::NR, ::pgb_host::launch_bdf<M, float>, ::pgb_host::launch_bdf<M, double>, \
         ::pgb_host::launch_null<M>, pgb::bdf_smem_per_thread<M, float>(),                    \
-        pgb::bdf_smem_per_thread<M, double>(), pgb::bdf_smem_per_thread<M, float, true>(),   \
-        pgb::bdf_smem_per_thread<M, double, true>(), ::pgb_host::rates_entry<M>,             \
+        pgb::bdf_smem_per_thread<M, double>(),                                               \
+        pgb::bdf_smem_per_thread<M, float, pgb::LAYOUT_Z_GLOBAL>(),                          \
+        pgb::bdf_smem_per_thread<M, double, pgb::LAYOUT_Z_GLOBAL>(),                         \
+        pgb::bdf_smem_per_thread<M, float, 3>(), pgb::bdf_smem_per_thread<M, double, 3>(),   \
+        ::pgb_host::rates_entry<M>,                                                          \
         ::pgb_host::h2t_entry<M>                                                             \
   }
 

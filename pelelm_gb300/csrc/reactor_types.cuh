@@ -52,6 +52,7 @@ struct ReactParams {
   unsigned long long* next_cell;  // work queue head (device scratch)
   ReactStats* stats;              // device scratch
   void* lu_scratch;               // per-thread Jacobian/LU slices in global memory, or null
+  void* z_scratch;                // per-thread Nordsieck histories in global memory, or null
 };
 
 }  // namespace pgb

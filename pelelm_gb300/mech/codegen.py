@@ -100,15 +100,20 @@ def gen_header(m: Mechanism) -> str:
     e(f"#ifndef {guard}")
     e(f"#define {guard}")
     e('#include "../mech_common.cuh"')
+    e(f'#include "tab_{m.name}.cuh"')
     e()
     e("namespace pgb {")
     e(f"struct Mech_{m.name} {{")
     e.ind += 1
+    e(f"using Tab = tab_{m.name}::Tables;")
     e(f"static constexpr int NS = {ns};")
     e(f"static constexpr int NR = {nr};")
     e(f"static constexpr int N = {N};")
     e(f'static constexpr const char* NAME = "{m.name}";')
     e(f"static constexpr bool SYNTHETIC = {'true' if m.synthetic else 'false'};")
+    e("// small mechanisms use the unrolled RHS / Jacobian below, larger ones the table-driven loops")
+    e(f"static constexpr bool JAC_TABLE = {'true' if ns > 12 else 'false'};")
+    e(f"static constexpr bool RHS_TABLE = {'true' if ns > 12 else 'false'};")
     e()
     # ---------------------------------------------------------------- molecular weights
     e("__host__ __device__ static constexpr double W(int k) {")
@@ -445,3 +450,105 @@ if __name__ == "__main__":
     import sys
     here = os.path.dirname(os.path.abspath(__file__))
     main(sys.argv[1] if len(sys.argv) > 1 else os.path.join(here, "..", "csrc", "gen"))
+
+
+# ---------------------------------------------------------------------------- tables
+def gen_tables(m: Mechanism) -> str:
+    """Constant-memory tables of a mechanism for the table-driven Jacobian (and any other
+    loop-over-reactions kernel): per-species W, NASA-7 sets, per-reaction Arrhenius data,
+    stoichiometry as species slots (a species with coefficient 2 occupies two slots), sparse
+    third-body efficiencies and Troe parameters."""
+    ns = m.ns
+    idx = {s.name: i for i, s in enumerate(m.species)}
+    tb_rows, troe_rows = [], []
+    rx = []
+    for r in m.reactions:
+        rs = [idx[s] for s, nu in r.reactants.items() for _ in range(nu)]
+        ps = [idx[s] for s, nu in r.products.items() for _ in range(nu)]
+        assert len(rs) <= 3 and len(ps) <= 3
+        kind = {"elementary": 0, "three_body": 1, "falloff": 2}[r.kind]
+        tb = -1
+        if r.kind != "elementary":
+            tb = len(tb_rows)
+            effs = [(idx[s], e - 1.0) for s, e in r.efficiencies.items() if e != 1.0]
+            tb_rows.append(effs)
+        tr = -1
+        if r.kind == "falloff":
+            tr = len(troe_rows)
+            lnA0 = math.log(r.low.A)
+            t = r.troe or []
+            troe_rows.append((lnA0, r.low.beta, -r.low.Ea / R_CAL, len(t),
+                              (1.0 - t[0]) if t else 0.0, (-1.0 / t[1]) if t else 0.0,
+                              t[0] if t else 0.0, (-1.0 / t[2]) if t else 0.0,
+                              (-t[3]) if len(t) > 3 else 0.0))
+        dnu = sum(r.products.values()) - sum(r.reactants.values())
+        rx.append((math.log(r.rate.A), r.rate.beta, -r.rate.Ea / R_CAL, kind, int(r.reversible),
+                   rs, ps, dnu, tb, tr))
+    maxeff = max([len(t) for t in tb_rows] + [1])
+    e = _Emitter()
+    e(f"// GENERATED by pelelm_gb300/mech/codegen.py (tables) from pelelm_gb300/data/{m.name}.json.")
+    guard = f"PGB_TAB_{m.name.upper()}_CUH"
+    e(f"#ifndef {guard}")
+    e(f"#define {guard}")
+    e('#include "../mech_tables.cuh"')
+    e("namespace pgb {")
+    e(f"namespace tab_{m.name} {{")
+    e(f"constexpr int NS = {ns}, NR = {m.nr}, NTB = {max(1, len(tb_rows))}, NTROE = {max(1, len(troe_rows))}, MAXEFF = {maxeff};")
+    for R, suf, cast in (("double", "D", lambda x: _f(x)), ("float", "F", lambda x: _f(x) + "f")):
+        e(f"__device__ __constant__ TabSpecies<{R}> kSpecies{suf}[NS] = {{")
+        def gco(a):
+            return [a[0], -a[1] / 2, -a[2] / 6, -a[3] / 12, -a[4] / 20, a[5], -a[6]]
+
+        def hco(a):
+            return [a[0], a[1] / 2, a[2] / 3, a[3] / 4, a[4] / 5, a[5]]
+
+        for sp_ in m.species:
+            arrs = [sp_.low, sp_.high, gco(sp_.low), gco(sp_.high), hco(sp_.low), hco(sp_.high)]
+            body = ", ".join("{" + ", ".join(cast(a_) for a_ in arr) + "}" for arr in arrs)
+            e(f"  {{{cast(sp_.W)}, {cast(1.0 / sp_.W)}, {cast(sp_.Tmid)}, {body}}},")
+        e("};")
+        e(f"__device__ __constant__ TabReaction<{R}> kReactions{suf}[NR] = {{")
+        for (lnA, beta, mear, kind, rev, rs, ps, dnu, tb, tr) in rx:
+            rsl = ", ".join(str(x) for x in (rs + [0, 0, 0])[:3])
+            psl = ", ".join(str(x) for x in (ps + [0, 0, 0])[:3])
+            e(f"  {{{cast(lnA)}, {cast(beta)}, {cast(mear)}, {kind}, {rev}, {len(rs)}, {len(ps)}, {{{rsl}}}, {{{psl}}}, {dnu}, {tb}, {tr}}},")
+        e("};")
+        e(f"__device__ __constant__ TabThirdBody<{R}> kThirdBody{suf}[NTB] = {{")
+        if not tb_rows:
+            e(f"  {{0, {{0}}, {{{cast(0.0)}}}}},")
+        for effs in tb_rows:
+            sp = ", ".join(str(k) for k, _ in effs) or "0"
+            ev = ", ".join(cast(v) for _, v in effs) or cast(0.0)
+            e(f"  {{{len(effs)}, {{{sp}}}, {{{ev}}}}},")
+        e("};")
+        e(f"__device__ __constant__ TabTroe<{R}> kTroe{suf}[NTROE] = {{")
+        if not troe_rows:
+            e("  {" + ", ".join([cast(0.0)] * 3 + ["0"] + [cast(0.0)] * 5) + "},")
+        for t in troe_rows:
+            e("  {" + ", ".join(cast(v) if isinstance(v, float) else str(v) for v in t) + "},")
+        e("};")
+    e("struct Tables {")
+    e(f"  static constexpr int NS = {ns}, NR = {m.nr};")
+    for nm, typ, arr in (("sp", "TabSpecies", "kSpecies"), ("rx", "TabReaction", "kReactions"),
+                         ("tb", "TabThirdBody", "kThirdBody"), ("troe", "TabTroe", "kTroe")):
+        e(f"  template <class R> __device__ static const {typ}<R>& {nm}(int i) {{")
+        e(f"    if constexpr (sizeof(R) == sizeof(double)) return {arr}D[i]; else return {arr}F[i];")
+        e("  }")
+    e("};")
+    e(f"}}  // namespace tab_{m.name}")
+    e("}  // namespace pgb")
+    e(f"#endif  // {guard}")
+    return e.text()
+
+
+def write_tables(outdir: str, names=("lidryer_syn", "drm19_syn")):
+    from ..workloads import load_mechanism
+    for n in names:
+        text = gen_tables(load_mechanism(n))
+        path = os.path.join(outdir, f"tab_{n}.cuh")
+        if os.path.exists(path):
+            with open(path) as f:
+                if f.read() == text:
+                    continue
+        with open(path, "w") as f:
+            f.write(text)

@@ -47,7 +47,8 @@ def _run_both(torch, oracle_mod, cfg, n, seed, precision, sides):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("cfgname,n,sides", [("lidryer_32cube", 4096, [16]),
-                                             ("lidryer_amr120", 2048, [8, 8, 8, 8])])
+                                             ("lidryer_amr120", 2048, [8, 8, 8, 8]),
+                                             ("drm19_2M", 1024, [8, 8])])
 def test_react_fp64_matches_oracle(native_lib, oracle_mod, cuda, cfgname, n, sides):
     """Plain method (FP64 Jacobian and LU) against the oracle at the same rtol/atol."""
     precision = "fp64"
@@ -66,7 +67,8 @@ def test_react_fp64_matches_oracle(native_lib, oracle_mod, cuda, cfgname, n, sid
         "nfail": int(nfail), "nfail_oracle": int(nfail_o)})
     assert nfail == 0 and nfail_o == 0
     assert np.all(FCg > 0)
-    np.testing.assert_allclose(rEg, rEo, rtol=1e-14, atol=0)
+    # rho h crosses zero for fuel-rich CH4/air, so judge it on the scale of the field
+    np.testing.assert_allclose(rEg, rEo, rtol=1e-14, atol=1e-14 * np.abs(rEo).max())
     assert relT.max() <= 1e-6, f"T rel err {relT.max():.3e}"
     assert ratio.max() <= 1.0, f"rhoY err / (atol + rtol|rhoY|) = {ratio.max():.3e}"
     # same algorithm in the same precision: step/RHS counts agree on almost every cell
@@ -75,7 +77,8 @@ def test_react_fp64_matches_oracle(native_lib, oracle_mod, cuda, cfgname, n, sid
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("cfgname,n,sides", [("lidryer_32cube", 4096, [16]),
-                                             ("lidryer_amr120", 2048, [8, 8, 8, 8])])
+                                             ("lidryer_amr120", 2048, [8, 8, 8, 8]),
+                                             ("drm19_2M", 1024, [8, 8])])
 def test_react_mixed_accuracy_vs_tight_oracle(native_lib, oracle_mod, cuda, cfgname, n, sides):
     """Mixed precision (FP32 Jacobian/LU preconditioner, FP64 rates, residual, error test and
     step control) takes different Newton iterates than the FP64 path, so it is judged the way
