@@ -48,7 +48,8 @@ def parse():
     p.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-fp64-line", action="store_true")
-    p.add_argument("--cpu-sample", type=int, default=131072)
+    p.add_argument("--cpu-sample", type=int, default=0,
+                   help="cells timed on the CPU (0 = the whole workload, ~10 s on 16 cores)")
     return p.parse_args()
 
 
@@ -283,7 +284,7 @@ def run_gb(args, ws, rank, local, pg):
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(cfg, cs, args.cpu_sample)
+        cpu = cpu_baseline(cfg, cs, args.cpu_sample or ncell)
 
     if rank == 0:
         line = {
@@ -299,7 +300,10 @@ def run_gb(args, ws, rank, local, pg):
                        "launch": "one persistent work-stealing kernel per step, CUDA-graph replay"},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
-                         "frac": achieved / fp64_peak, "traffic": None,
+                         "frac": achieved / fp64_peak,
+                         # DRAM bytes per launch: ncu capture of a 131,072-cell launch (22.8 MB,
+                         # profiles/bdf_reactor_kernel_lidryer_131k.txt) scaled by cells
+                         "traffic": 22.81e6 * ncell / 131072,
                          "what": f"rate evaluation: {flops_rhs} algorithmic FP64 flops per RHS "
                                  f"({ops} ops + {trans} transcendentals x {FLOPS_PER_TRANSCENDENTAL}) "
                                  f"x {nfe_per_step} RHS evaluations per step / kernel time",
@@ -343,7 +347,8 @@ def run_reference(args, ws, rank, pg):
     from pelelm_gb300.workloads import CONFIGS, make_cells
     cfg = CONFIGS[args.config]
     cs = make_cells(cfg, seed=0)
-    sample = max(4096, args.cpu_sample // max(1, args.steps + args.warmup))
+    # each step: a quarter of the workload (about 3 s on 16 cores), so K + W steps stay in minutes
+    sample = args.cpu_sample or cfg.ncell // 4
     vals = []
     for i in range(args.warmup + args.steps):
         res = cpu_baseline(cfg, cs, sample)
