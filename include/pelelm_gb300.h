@@ -139,6 +139,31 @@ int pgb_react_boxes_noalloc(const char* mechanism, const pgb_box_view* views, in
                             double dt_react, double rtol, double atol, int max_order, int max_steps,
                             int fp64, void* stream, pgb_stats* stats);
 
+/* ---- Learned surrogate: BF16 tensor-core building blocks (FP32 accumulation). No counterpart in
+ * the reference: they train and evaluate the MLP that predicts a cell's (dY, dT) over dt_react.
+ * All pointers are device memory; bf16 arrays are passed as void*. ---- */
+
+/* C[m][n] = act(sum_k A[m][k] B[n][k] + bias[n]); A (M x K, lda), B (N x K, ldb) row-major BF16;
+ * K % 32 == 0. Writes the FP32 pre-activation to `pre`, and/or the result as BF16 (`out_bf16`) /
+ * FP32 (`out_f32`), all with leading dimension ldo; columns >= n_valid are written as 0.
+ * act: 0 identity, 1 GELU (tanh form). */
+int pgb_mlp_gemm_nt(const void* A, int lda, const void* B, int ldb, int M, int N, int K,
+                    const float* bias, int act, float* pre, void* out_bf16, float* out_f32, int ldo,
+                    int n_valid, void* stream);
+/* out (cols x rows, ldo) = in^T (rows x cols, ldi), BF16. */
+int pgb_mlp_transpose_bf16(const void* in, int rows, int cols, int ldi, void* out, int ldo, void* stream);
+/* dZ = dA * GELU'(pre), n elements (BF16 out, optional FP32 copy dZf). */
+int pgb_mlp_gelu_backward(const float* dA, const float* pre, void* dZ, float* dZf, long long n, void* stream);
+/* MSE over the first n_valid of ld columns: dY = 2 (Y - T) / (M n_valid) (FP32 and BF16), *loss += sum d^2. */
+int pgb_mlp_mse_grad(const float* Y, const float* T, int M, int ld, int n_valid, float* dYf, void* dY,
+                     float* loss, void* stream);
+/* db[n] = sum_m dZ[m][n]. */
+int pgb_mlp_bias_grad(const float* dZ, int M, int N, int ld, float* db, void* stream);
+/* Adam step `step` (>= 1) on FP32 parameters p with moments m, v; refreshes the BF16 copy p_bf16. */
+int pgb_mlp_adam(float* p, const float* g, float* m, float* v, void* p_bf16, long long n, float lr,
+                 float b1, float b2, float eps, int step, void* stream);
+int pgb_mlp_f32_to_bf16(const float* in, void* out, long long n, void* stream);
+
 /* Measures the device's FP64 FMA throughput in TFLOP/s (2 flops per FMA). No counterpart in
  * the reference: a measurement utility giving the roofline denominator of the FP64-bound
  * reactor kernels. */

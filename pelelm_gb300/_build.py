@@ -21,7 +21,7 @@ BUILD = os.path.join(PKG, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-std=c++17", "-O3", "-lineinfo", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
            "-Xcompiler", "-O2"]
-UNITS = ["reactor.cu", "peak.cu", "noalloc.cu", "mech_lidryer_syn.cu", "mech_drm19_syn.cu"]
+UNITS = ["reactor.cu", "peak.cu", "noalloc.cu", "mlp.cu", "mech_lidryer_syn.cu", "mech_drm19_syn.cu"]
 
 
 def nvcc() -> str:

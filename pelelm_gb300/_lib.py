@@ -49,6 +49,15 @@ EXPORTS = {
     "pgb_reaction_rates": (C.c_int, [C.c_char_p, C.POINTER(BoxView), C.POINTER(Array4), _vp]),
     "pgb_rhoh_to_temp": (C.c_int, [C.c_char_p, C.POINTER(BoxView), C.c_double, C.c_double, _vp]),
     "pgb_fp64_peak_tflops": (C.c_int, [C.c_int, C.POINTER(C.c_double)]),
+    "pgb_mlp_gemm_nt": (C.c_int, [_vp, C.c_int, _vp, C.c_int, C.c_int, C.c_int, C.c_int, _vp, C.c_int,
+                                  _vp, _vp, _vp, C.c_int, C.c_int, _vp]),
+    "pgb_mlp_transpose_bf16": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _vp, C.c_int, _vp]),
+    "pgb_mlp_gelu_backward": (C.c_int, [_vp, _vp, _vp, _vp, C.c_longlong, _vp]),
+    "pgb_mlp_mse_grad": (C.c_int, [_vp, _vp, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _vp]),
+    "pgb_mlp_bias_grad": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _vp, _vp]),
+    "pgb_mlp_adam": (C.c_int, [_vp, _vp, _vp, _vp, _vp, C.c_longlong, C.c_float, C.c_float, C.c_float,
+                               C.c_float, C.c_int, _vp]),
+    "pgb_mlp_f32_to_bf16": (C.c_int, [_vp, _vp, C.c_longlong, _vp]),
     "pgb_react_boxes_noalloc": (C.c_int, [C.c_char_p, C.POINTER(BoxView), C.c_int, C.c_double,
                                           C.c_double, C.c_double, C.c_int, C.c_int, C.c_int, _vp,
                                           C.POINTER(Stats)]),
