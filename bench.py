@@ -1,23 +1,28 @@
 #!/usr/bin/env python
-"""Chemistry cells/sec per dt_react of the GB300 reactor on the AMR-like LiDryer workload.
+"""Chemistry cells/sec per dt_react: learned surrogate + BDF fallback vs the plain GPU BDF.
 
-Workload (one "step" = one advance of every cell of every box over dt_react):
-  LiDryer-shaped H2/O2 mechanism (9 species, 21 reactions; synthetic, structure-matched),
-  120 boxes with sides in {8,16,32,64} = 2,154,496 cells, dt_react = 1e-5 s, rtol 1e-6,
-  atol 1e-10, N(0, 1e2^2) kg/m^3/s species forcing (realizable, zero net mass) and
+Default workload (one "step" = one advance of every cell of every box over dt_react):
+  drm19-shaped CH4/air mechanism (21 species, 84 reactions; synthetic, structure-matched),
+  48 x 32^3 + 128 x 16^3 = 2^21 cells, T = 300 + 1900 c, phi ~ U[0.6, 1.4], dt_react = 1e-5 s,
+  rtol 1e-6, atol 1e-10, N(0, 1e2^2) kg/m^3/s species forcing (realizable, zero net mass) and
   N(0, 1e8^2) W/m^3 energy forcing. Inputs are seeded synthetic states (no dataset exists).
+  The reactor runs the trained surrogate (pelelm_gb300/data/drm19_syn.pgbs) over every cell;
+  cells failing its checks, plus a 1% audit sample, are advanced by the GPU BDF in the same
+  CUDA graph. The same workload through the plain GPU BDF, the share of the step in each
+  kernel and the error of the result against the FP64 oracle at rtol 1e-10 (stratified
+  subsample) are reported beside it. --config lidryer_amr120 --surrogate none gives the plain
+  BDF on the 2,154,496-cell LiDryer-shaped AMR workload.
 
 Arms:
-  default            the GB300 reactor through its C ABI (pgb_reactor_react_boxes), one
-                     persistent work-stealing launch per step over all boxes.
+  default            the GB300 reactor through its C ABI (pgb_reactor_react_boxes).
   --impl reference   the CPU CVODE-class restatement of the reference reactor (the oracle) on
                      all host cores, timed on a bounded sample of the same workload.
 
 Timing: W warm-up steps, then K timed steps, each bracketed by a barrier and
-torch.cuda.synchronize() with CUDA events on the launch stream; the device state (577 MB)
-exceeds L2 (129 MB) and is restored from a pristine copy between steps (untimed). `e2e`
-repeats the steps from pinned host memory with the H2D input copies and D2H result copies
-inside the timed region.
+torch.cuda.synchronize() with CUDA events on the launch stream; the device state (1.2 GB for
+drm19_2M) exceeds L2 (129 MB) and is restored from a pristine copy between steps (untimed).
+`e2e` repeats the steps from pinned host memory with the H2D input copies and D2H result
+copies inside the timed region.
 """
 from __future__ import annotations
 
@@ -34,17 +39,21 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "chemistry cells/sec per dt_react"
+METRIC = "chemistry cells/sec per dt_react: surrogate+fallback vs GPU BDF at \u22641 K error"
 UNIT = "cells/s"
 
 
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--steps", type=int, default=2)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb", choices=["gb", "reference"])
-    p.add_argument("--config", default="lidryer_amr120")
+    p.add_argument("--config", default="drm19_2M")
+    p.add_argument("--surrogate", default="pelelm_gb300/data/drm19_syn.pgbs",
+                   help="trained surrogate file, or 'none' for the plain GPU BDF")
+    p.add_argument("--no-error-check", action="store_true")
+    p.add_argument("--error-sample", type=int, default=4096)
     p.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-fp64-line", action="store_true")
@@ -185,11 +194,15 @@ def run_gb(args, ws, rank, local, pg):
     cfg, cs, lay, arenas = build_workload(args.config, seed=rank)
     mech = load_mechanism(cfg.mech)
     ns, ncell = mech.ns, lay.ncell
+    surrogate = args.surrogate if args.surrogate != "none" else None
+    if surrogate and not os.path.isabs(surrogate):
+        surrogate = os.path.join(ROOT, surrogate)
     lib = _lib.lib()
     import ctypes as C
     peak = C.c_double()
     _lib.check(lib.pgb_fp64_peak_tflops(20000, C.byref(peak)), "fp64 peak")
     fp64_peak = peak.value
+    peaks = measured_peaks()
 
     stream = torch.cuda.Stream()
     fields = ["rY", "rY_src", "T", "rEner", "rEner_src"]
@@ -197,10 +210,10 @@ def run_gb(args, ws, rank, local, pg):
     work = {k: v.clone() for k, v in pristine.items()}
     work["FC"] = torch.zeros(ncell, dtype=torch.float64, device="cuda")
     views = box_views(torch, lay, work, ns)
+    base_opts = f"ode.rtol={cfg.rtol} ode.atol={cfg.atol} gb.graph=1"
 
-    def make_reactor(precision):
-        r = ReactorBase.create("ReactorCvode", cfg.mech,
-                               f"ode.rtol={cfg.rtol} ode.atol={cfg.atol} gb.precision={precision} gb.graph=1")
+    def make_reactor(precision, extra=""):
+        r = ReactorBase.create("ReactorCvode", cfg.mech, f"{base_opts} gb.precision={precision} {extra}")
         r.init(2, 1)
         return r
 
@@ -209,7 +222,7 @@ def run_gb(args, ws, rank, local, pg):
             work[k].copy_(pristine[k])
         work["FC"].zero_()
 
-    def timed_steps(r, nsteps, warm):
+    def timed_steps(r, nsteps, warm, clocks=True):
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(nsteps)]
         for _ in range(warm):
             restore()
@@ -218,7 +231,8 @@ def run_gb(args, ws, rank, local, pg):
             torch.cuda.synchronize()
         total = 0.0
         sampler = ClockSampler(dev_index)
-        sampler.start()
+        if clocks:
+            sampler.start()
         for i in range(nsteps):
             restore()
             torch.cuda.synchronize()
@@ -230,29 +244,26 @@ def run_gb(args, ws, rank, local, pg):
             torch.cuda.synchronize()
             barrier(pg, dev_index)
             total += ev[i][0].elapsed_time(ev[i][1]) / 1e3
-        clocks = sampler.stop()
-        return total, clocks, r.stats()
+        return total, (sampler.stop() if clocks else None), r.stats()
 
-    r = make_reactor(args.precision)
-    t_kern, clocks, st = timed_steps(r, args.steps, args.warmup)
-    t_max = allmax(pg, t_kern)
-    cells_all = allsum(pg, float(ncell * args.steps))
-    value = cells_all / t_max
+    sg_opts = f"gb.surrogate={surrogate}" if surrogate else ""
+    r = make_reactor(args.precision, sg_opts)
+    t_step, clocks, st = timed_steps(r, args.steps, args.warmup)
+    sst = r.surrogate_stats() if surrogate else None
+    t_max = allmax(pg, t_step)
+    value = allsum(pg, float(ncell * args.steps)) / t_max
     ms_per_step = 1e3 * t_max / args.steps
-    nfe_per_step = st["nfe"]
-    flops_rhs = rhs_flops(mech)
-    ops, trans = rhs_ops(mech)
-    achieved = flops_rhs * nfe_per_step / (t_kern / args.steps) / 1e12
-    hist = st["hist"]
+    out_state = {k: work[k].clone() for k in ("rY", "T", "FC")} if surrogate else None
 
-    # ---- e2e: pinned host inputs -> H2D -> advance -> D2H of the results, all timed
+    # ---- e2e: pinned host inputs -> H2D -> advance -> D2H of the results, all timed (the
+    # reactor is warm from the steps above: one untimed e2e pass, then K timed)
     host_in = {k: torch.from_numpy(arenas[k]).pin_memory() for k in fields}
     out_fields = ["rY", "T", "rEner", "FC"]
     host_out = {k: torch.empty_like(work[k], device="cpu").pin_memory() for k in out_fields}
     h2d = sum(v.numel() * 8 for v in host_in.values())
     d2h = sum(v.numel() * 8 for v in host_out.values())
     e2e_total = 0.0
-    for i in range(args.warmup + args.steps):
+    for i in range(1 + args.steps):
         torch.cuda.synchronize()
         barrier(pg, dev_index)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -267,57 +278,185 @@ def run_gb(args, ws, rank, local, pg):
             e1.record(stream)
         torch.cuda.synchronize()
         barrier(pg, dev_index)
-        if i >= args.warmup:
+        if i >= 1:
             e2e_total += e0.elapsed_time(e1) / 1e3
     e2e_value = allsum(pg, float(ncell * args.steps)) / allmax(pg, e2e_total)
-    nfail = int(st["nfail"])
     r.close()
 
+    flops_rhs = rhs_flops(mech)
+    ops, trans = rhs_ops(mech)
     extra = {}
-    if not args.no_fp64_line and args.precision != "fp64":
-        r64 = make_reactor("fp64")
-        t64, _, st64 = timed_steps(r64, max(1, min(args.steps, 2)), 1)
-        extra["fp64_plain"] = {"cells_per_s": ncell * max(1, min(args.steps, 2)) / t64,
-                               "ms_per_step": 1e3 * t64 / max(1, min(args.steps, 2)),
-                               "nfe_per_step": st64["nfe"]}
-        r64.close()
+    if surrogate:
+        # the same workload through the plain GPU BDF (same precision), and the surrogate kernel
+        # alone (every gate open: no cell reaches the BDF) to split the step between kernels
+        rp = make_reactor(args.precision)
+        n_plain = max(1, min(args.steps, 2))
+        t_plain, _, st_plain = timed_steps(rp, n_plain, 1, clocks=False)
+        rp.close()
+        ra = make_reactor(args.precision, sg_opts + " gb.sg.audit=0 gb.sg.mis=1e30 gb.sg.cons=1e30 "
+                          "gb.sg.disT=1e30 gb.sg.disY=1e30 gb.sg.neg=1e30 gb.sg.ood_margin=1e30")
+        t_sg, _, _ = timed_steps(ra, 3, 2, clocks=False)
+        t_sg /= 3
+        ra.close()
+        plain_cps = allsum(pg, float(ncell * n_plain)) / allmax(pg, t_plain)
+        t_bdf = max(t_step / args.steps - t_sg, 1e-9)
+        nfe = st["nfe"]
+        achieved = flops_rhs * nfe / t_bdf / 1e12
+        from pelelm_gb300.surrogate import read_pgbs
+        d = read_pgbs(surrogate)
+        mlp_flops = 2.0 * d["nmodel"] * sum(int(d["dims"][l]) * int(d["dims"][l + 1]) for l in range(d["nlayer"]))
+        extra["plain_gpu_bdf"] = {"cells_per_s": plain_cps, "ms_per_step": 1e3 * t_plain / n_plain,
+                                  "nfe_per_cell": st_plain["nfe"] / ncell, "precision": args.precision}
+        extra["speedup_vs_plain_gpu_bdf"] = value / plain_cps
+        extra["surrogate"] = {
+            "file": os.path.relpath(surrogate, ROOT), "members": d["nmodel"],
+            "accepted_frac": sst["accept"] / max(sst["ncell"], 1),
+            "fallback_frac": sst["fallback"] / max(sst["ncell"], 1),
+            "audit_frac": sst["audit"] / max(sst["ncell"], 1), "audit_bad": sst["audit_bad"],
+            "audit_max_dT_K": sst["audit_max_dT"], "audit_max_dY": sst["audit_max_dY"],
+            "rejected_by": {k: sst[k] for k in ("ood", "mis", "cons", "ens", "neg")},
+            "bdf_work_saved_frac": 1.0 - nfe / max(st_plain["nfe"], 1),
+            "kernel_ms": {"surrogate_inference": 1e3 * t_sg, "bdf_fallback_and_audit": 1e3 * t_bdf},
+            "inference_roofline": {"bound": "tensor", "unit": "TFLOP/s",
+                                   "achieved": mlp_flops * ncell / t_sg / 1e12,
+                                   "peak": peaks.get("bf16_tflops"),
+                                   "frac": (mlp_flops * ncell / t_sg / 1e12 / peaks["bf16_tflops"])
+                                   if peaks.get("bf16_tflops") else None,
+                                   "what": f"{mlp_flops:.0f} padded MMA flops per cell (ensemble of "
+                                           f"{d['nmodel']}) / surrogate kernel time incl. featurise+gates",
+                                   "peak_source": "MEASURED_PEAKS.json bf16 (cuBLAS burst) of measured"},
+        }
+        if rank == 0 and not args.no_error_check:
+            extra["error_vs_fp64_oracle"] = error_vs_oracle(cfg, cs, lay, out_state, args.error_sample)
+        dominant = "bdf_reactor_kernel (fallback cells)"
+    else:
+        nfe = st["nfe"]
+        achieved = flops_rhs * nfe / (t_step / args.steps) / 1e12
+        dominant = "bdf_reactor_kernel"
+        if not args.no_fp64_line and args.precision != "fp64":
+            r64 = make_reactor("fp64")
+            t64, _, st64 = timed_steps(r64, max(1, min(args.steps, 2)), 1, clocks=False)
+            extra["fp64_plain"] = {"cells_per_s": ncell * max(1, min(args.steps, 2)) / t64,
+                                   "ms_per_step": 1e3 * t64 / max(1, min(args.steps, 2)),
+                                   "nfe_per_step": st64["nfe"]}
+            r64.close()
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(cfg, cs, args.cpu_sample or ncell)
+        cpu = cpu_baseline(cfg, cs, args.cpu_sample or default_cpu_sample(cfg))
 
     if rank == 0:
+        hist = st["hist"]
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f64+f32",
-            "data": "synthetic (seeded states; synthetic structure-matched LiDryer-shaped mechanism)",
-            "config": {"workload": "lidryer_amr120: LiDryer-shaped H2/O2 (9 sp, 21 rx), 120 boxes "
-                                   "{8,16,32,64}^3 = 2,154,496 cells, dt_react 1e-5 s, rtol 1e-6, "
-                                   "atol 1e-10, realizable N(0,1e2^2) kg/m^3/s + N(0,1e8^2) W/m^3 forcing",
+            "data": f"synthetic (seeded states; synthetic structure-matched {mech.name} mechanism)",
+            "config": {"workload": WORKLOAD_TEXT.get(args.config, args.config) +
+                       (" | learned surrogate (4x256 GELU BF16 MLP ensemble, fused inference) with "
+                        "BDF fallback and 1% audit" if surrogate else " | plain GPU BDF"),
                        "precision": args.precision, "cells_per_gpu": ncell,
-                       "l2": "inputs (577 MB of state) larger than L2; state restored between steps",
-                       "launch": "one persistent work-stealing kernel per step, CUDA-graph replay"},
+                       "l2": f"inputs ({ncell * (3 * ns + 5) * 8 / 1e6:.0f} MB of state) larger than L2; "
+                             "state restored between steps",
+                       "launch": "surrogate kernel -> persistent work-stealing BDF on the device fallback "
+                                 "list -> audit kernel, one CUDA graph per step" if surrogate else
+                                 "one persistent work-stealing kernel per step, CUDA-graph replay"},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
                          "frac": achieved / fp64_peak,
-                         # DRAM bytes per launch: ncu capture of a 131,072-cell launch (22.8 MB,
-                         # profiles/bdf_reactor_kernel_lidryer_131k.txt) scaled by cells
-                         "traffic": 22.81e6 * ncell / 131072,
+                         # DRAM bytes per launch from an ncu capture of a smaller launch of the same
+                         # kernel, scaled by cells (profiles/)
+                         "traffic": TRAFFIC_PER_CELL.get(cfg.mech, 0.0) * ncell if not surrogate else None,
+                         "kernel": dominant,
                          "what": f"rate evaluation: {flops_rhs} algorithmic FP64 flops per RHS "
                                  f"({ops} ops + {trans} transcendentals x {FLOPS_PER_TRANSCENDENTAL}) "
-                                 f"x {nfe_per_step} RHS evaluations per step / kernel time",
+                                 f"x {nfe} RHS evaluations per step / BDF kernel time",
                          "peak_source": "measured in this run: pgb_fp64_peak_tflops (DFMA, full grid)"},
             "stats": {"nst_per_cell": st["nst"] / ncell, "nfe_per_cell": st["nfe"] / ncell,
-                      "nje_per_cell": st["nje"] / ncell, "max_steps_cell": st["max_nst"], "nfail": nfail,
+                      "nje_per_cell": st["nje"] / ncell, "max_steps_cell": st["max_nst"], "nfail": int(st["nfail"]),
                       "steps_hist_log2": hist},
             "clocks": clocks,
-            "gpu_launches": args.steps,
+            "gpu_launches": args.steps * (3 if surrogate else 1),
             **extra,
         }
         if cpu:
             line["cpu_baseline"] = cpu
         print(json.dumps(line), flush=True)
+
+
+WORKLOAD_TEXT = {
+    "lidryer_amr120": "lidryer_amr120: LiDryer-shaped H2/O2 (9 sp, 21 rx), 120 boxes {8,16,32,64}^3 = "
+                      "2,154,496 cells, dt_react 1e-5 s, rtol 1e-6, atol 1e-10, realizable N(0,1e2^2) "
+                      "kg/m^3/s + N(0,1e8^2) W/m^3 forcing",
+    "drm19_2M": "drm19_2M: drm19-shaped CH4/air (21 sp, 84 rx), 48x32^3 + 128x16^3 = 2^21 cells, "
+                "T = 300 + 1900 c, phi ~ U[0.6,1.4], dt_react 1e-5 s, rtol 1e-6, atol 1e-10, forcing as "
+                "lidryer_amr120",
+    "drm19_4M": "drm19_4M: drm19-shaped CH4/air (21 sp, 84 rx), the drm19_2M state distribution on "
+                "96x32^3 + 256x16^3 = 2^22 cells, dt_react 1e-5 s, rtol 1e-6, atol 1e-10",
+}
+
+# DRAM bytes per cell of one BDF launch (ncu, scaled from the captured launch)
+TRAFFIC_PER_CELL = {"lidryer_syn": 22.81e6 / 131072}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+    except (OSError, ValueError):
+        return {}
+    out = {}
+    for k, v in d.items():
+        if isinstance(v, (int, float)):
+            out[k] = float(v)
+    return out
+
+
+def error_vs_oracle(cfg, cs, lay, out_state, sample):
+    """Error of the step's result against the FP64 oracle at rtol 1e-10 on a subsample stratified
+    by what the surrogate did (accepted cells and BDF cells, each spread uniformly over T)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from pelelm_gb300.workloads import from_box_arena, mech_path
+    O.build()
+    ns = cs.rY.shape[1]
+    rY = from_box_arena(lay, out_state["rY"].cpu().numpy(), ns)
+    T = from_box_arena(lay, out_state["T"].cpu().numpy(), 1)
+    FC = from_box_arena(lay, out_state["FC"].cpu().numpy(), 1)
+    acc = np.nonzero(FC == 0.0)[0]
+    fb = np.nonzero(FC != 0.0)[0]
+    idx = []
+    for grp in (acc, fb):
+        if grp.size:
+            order = grp[np.argsort(cs.T[grp], kind="stable")]
+            k = min(order.size, sample // 2 if acc.size and fb.size else sample)
+            idx.append(order[np.linspace(0, order.size - 1, k).astype(int)])
+    idx = np.unique(np.concatenate(idx))
+    om = O.OracleMech(mech_path(cfg.mech))
+    t0 = time.perf_counter()
+    tight = om.react(cs.rY[idx], cs.rYsrc[idx], cs.T[idx], cs.rE[idx], cs.rEsrc[idx], cs.mask[idx], cfg.dt,
+                     1e-10, 1e-14, max_steps=200000)
+    dt = time.perf_counter() - t0
+    Yg = rY[idx] / rY[idx].sum(1, keepdims=True)
+    Yo = tight[0] / tight[0].sum(1, keepdims=True)
+    eT = np.abs(T[idx] - tight[1])
+    eY = np.abs(Yg - Yo).max(1)
+    a = np.isin(idx, acc)
+
+    def summ(m):
+        if not m.any():
+            return None
+        return {"n": int(m.sum()), "max_dT_K": float(eT[m].max()), "p99_dT_K": float(np.percentile(eT[m], 99)),
+                "max_dY": float(eY[m].max()), "p99_dY": float(np.percentile(eY[m], 99))}
+
+    return {"oracle": "oracle/ C++ BDF, FP64, rtol 1e-10, atol 1e-14", "oracle_s": round(dt, 2),
+            "all": summ(np.ones_like(a)), "surrogate_cells": summ(a), "bdf_cells": summ(~a),
+            "within_1K_1e-4": bool(eT.max() <= 1.0 and eY.max() <= 1e-4)}
+
+
+def default_cpu_sample(cfg):
+    # about 10-30 s of CPU work on the box's 16 cores
+    return {"lidryer_syn": cfg.ncell, "drm19_syn": 131072}.get(cfg.mech, 65536)
 
 
 # ---------------------------------------------------------------- CPU (oracle) legs
@@ -347,8 +486,8 @@ def run_reference(args, ws, rank, pg):
     from pelelm_gb300.workloads import CONFIGS, make_cells
     cfg = CONFIGS[args.config]
     cs = make_cells(cfg, seed=0)
-    # each step: a quarter of the workload (about 3 s on 16 cores), so K + W steps stay in minutes
-    sample = args.cpu_sample or cfg.ncell // 4
+    # each step: a bounded sample (a few seconds on 16 cores), so K + W steps stay in minutes
+    sample = args.cpu_sample or default_cpu_sample(cfg) // 4
     vals = []
     for i in range(args.warmup + args.steps):
         res = cpu_baseline(cfg, cs, sample)
@@ -359,10 +498,11 @@ def run_reference(args, ws, rank, pg):
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * sample / value, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
-            "data": "synthetic (seeded states; synthetic structure-matched LiDryer-shaped mechanism)",
-            "config": {"workload": "lidryer_amr120 (bounded sample per step)", "cells_per_step": sample},
+            "data": f"synthetic (seeded states; synthetic structure-matched {cfg.mech} mechanism)",
+            "config": {"workload": WORKLOAD_TEXT.get(args.config, args.config) + " | CPU CVODE-class BDF "
+                                   "(bounded sample per step)", "cells_per_step": sample},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": f"{sample} cells per step, uniform subsample of the 2,154,496-cell "
+                             "sample": f"{sample} cells per step, uniform subsample of the {cfg.ncell}-cell "
                                        "workload; the reference's own CVODE reactor is not in the "
                                        "reference tree, so its C++ restatement (oracle/) runs"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}

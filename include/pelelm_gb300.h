@@ -63,7 +63,10 @@ typedef struct {
  * options: whitespace/semicolon separated key=value pairs — the reference's runtime keys
  * ode.rtol, ode.atol, cvode.max_order, cvode.solve_type, ode.analytical_jacobian,
  * peleLM.use_typ_vals_chem, plus ode.max_steps, gb.precision=fp64|mixed, gb.tpb, gb.graph=0|1,
- * gb.history=shared|global.
+ * gb.history=shared|global, gb.lu=shared|global, and gb.surrogate=<file> (learned surrogate
+ * with BDF fallback; no reference counterpart) with threshold overrides gb.sg.audit (audit
+ * fraction), gb.sg.mis [K], gb.sg.cons, gb.sg.disT [K], gb.sg.disY, gb.sg.neg,
+ * gb.sg.ood_margin, gb.sg.tol_T, gb.sg.tol_Y, gb.sg.models, gb.sg.seed.
  * Returns NULL on error. */
 pgb_reactor* pgb_reactor_create(const char* name, const char* mechanism, int reactor_type,
                                 const char* options);
@@ -88,6 +91,19 @@ int pgb_reactor_react_boxes(pgb_reactor* r, const pgb_box_view* views, int nbox,
 
 /* Waits for the last advance on its stream and returns its counters. */
 int pgb_reactor_get_stats(pgb_reactor* r, pgb_stats* out);
+
+/* Counters of the learned surrogate in the last advance (reactor created with gb.surrogate).
+ * No counterpart in the reference. ncell: unmasked cells; accept: cells written by the
+ * surrogate; fallback: cells advanced by the BDF (rejected + audited); ood/mis/cons/ens/neg:
+ * cells failing the out-of-distribution, enthalpy, element-conservation, ensemble and
+ * negativity checks (a cell may fail several); audit: accepted cells also advanced by the BDF
+ * for comparison; audit_bad: audited cells off by more than the audit tolerances; audit_max_*:
+ * largest |T| [K] and |Y| differences between surrogate and BDF over the audit sample. */
+typedef struct pgb_surrogate_stats {
+  unsigned long long ncell, accept, fallback, ood, mis, cons, ens, neg, audit, audit_bad;
+  double audit_max_dT, audit_max_dY;
+} pgb_surrogate_stats;
+int pgb_reactor_get_surrogate_stats(pgb_reactor* r, pgb_surrogate_stats* out);
 
 /* ReactorBase::close (Source/PeleLM.cpp:930) and destruction. */
 void pgb_reactor_close(pgb_reactor* r);
@@ -163,6 +179,13 @@ int pgb_mlp_bias_grad(const float* dZ, int M, int N, int ld, float* db, void* st
 int pgb_mlp_adam(float* p, const float* g, float* m, float* v, void* p_bf16, long long n, float lr,
                  float b1, float b2, float eps, int step, void* stream);
 int pgb_mlp_f32_to_bf16(const float* in, void* out, long long n, void* stream);
+/* First-layer weight for a split input: each FP32 row of W (rows x cols) is written to out
+ * (row stride ldo >= 2*cols) twice as BF16, at columns [0, cols) and [cols, 2*cols). */
+int pgb_mlp_dup_weight_bf16(const float* W, int rows, int cols, void* out, int ldo, void* stream);
+/* Splits FP32 rows x (row stride ldx) into BF16 high parts at out columns [0, cols) and BF16
+ * low parts (x - high) at columns [off, off + cols); row stride of out is ldo. */
+int pgb_mlp_split_rows_bf16(const float* x, int rows, int cols, int ldx, void* out, int ldo, int off,
+                            void* stream);
 
 /* Measures the device's FP64 FMA throughput in TFLOP/s (2 flops per FMA). No counterpart in
  * the reference: a measurement utility giving the roofline denominator of the FP64-bound

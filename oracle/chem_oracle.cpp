@@ -150,8 +150,12 @@ struct Core {
           dG = dG - sn.second * gRT[sn.first];
           if (need_derivs) dH = dH - sn.second * hRT[sn.first];
         }
-        // kr = kf / Kc,  Kc = exp(-dG) (P0/RT)^dnu
-        e.kr = kf * exp(dG - r.dnu * lnP0RT);
+        // kr = kf / Kc,  Kc = exp(-dG) (P0/RT)^dnu. The exponent is capped at 700 (exp stays
+        // finite): far below equilibrium at low T it overflows, and inf times an absent
+        // product's zero concentration would turn the rate of progress into NaN.
+        R arg = dG - r.dnu * lnP0RT;
+        if (value(arg) > 700.0) arg = R(700.0);
+        e.kr = kf * exp(arg);
         if (need_derivs) e.dlnkr = dlnkf - (dH - r.dnu) * invT;
       }
       R Pf = R(1.0), Pp = R(1.0);

@@ -21,7 +21,8 @@ BUILD = os.path.join(PKG, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-std=c++17", "-O3", "-lineinfo", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
            "-Xcompiler", "-O2"]
-UNITS = ["reactor.cu", "peak.cu", "noalloc.cu", "mlp.cu", "mech_lidryer_syn.cu", "mech_drm19_syn.cu"]
+UNITS = ["reactor.cu", "peak.cu", "noalloc.cu", "mlp.cu", "surrogate_io.cu", "mech_lidryer_syn.cu", "mech_drm19_syn.cu",
+         "mech_gri_syn.cu"]
 
 
 def nvcc() -> str:
@@ -34,8 +35,8 @@ def nvcc() -> str:
 def generate_sources() -> None:
     from .mech import codegen
     gen = os.path.join(CSRC, "gen")
-    codegen.main(gen, names=("lidryer_syn", "drm19_syn"))
-    codegen.write_tables(gen, names=("lidryer_syn", "drm19_syn"))
+    codegen.main(gen, names=("lidryer_syn", "drm19_syn", "gri_syn"))
+    codegen.write_tables(gen, names=("lidryer_syn", "drm19_syn", "gri_syn"))
     # the exp64 constants are committed (their generator needs mpmath, absent on some hosts)
     if not os.path.exists(os.path.join(gen, "exp64_table.cuh")):
         subprocess.check_call([sys.executable, os.path.join(CSRC, "gen_exp64.py")])

@@ -34,6 +34,12 @@ class Stats(C.Structure):
                 ("nfail", C.c_ulonglong), ("max_nst", C.c_ulonglong), ("hist", C.c_ulonglong * 16)]
 
 
+class SurrogateStats(C.Structure):
+    _fields_ = [(n, C.c_ulonglong) for n in ("ncell", "accept", "fallback", "ood", "mis", "cons", "ens", "neg",
+                                               "audit", "audit_bad")] + \
+               [("audit_max_dT", C.c_double), ("audit_max_dY", C.c_double)]
+
+
 EXPORTS = {
     "pgb_version": (C.c_int, []),
     "pgb_last_error": (C.c_int, [C.c_char_p, C.c_size_t]),
@@ -45,6 +51,7 @@ EXPORTS = {
     "pgb_reactor_react_boxes": (C.c_int, [_vp, C.POINTER(BoxView), C.c_int, C.c_double,
                                           C.c_double, _vp]),
     "pgb_reactor_get_stats": (C.c_int, [_vp, C.POINTER(Stats)]),
+    "pgb_reactor_get_surrogate_stats": (C.c_int, [_vp, C.POINTER(SurrogateStats)]),
     "pgb_reactor_close": (None, [_vp]),
     "pgb_reaction_rates": (C.c_int, [C.c_char_p, C.POINTER(BoxView), C.POINTER(Array4), _vp]),
     "pgb_rhoh_to_temp": (C.c_int, [C.c_char_p, C.POINTER(BoxView), C.c_double, C.c_double, _vp]),
@@ -58,6 +65,8 @@ EXPORTS = {
     "pgb_mlp_adam": (C.c_int, [_vp, _vp, _vp, _vp, _vp, C.c_longlong, C.c_float, C.c_float, C.c_float,
                                C.c_float, C.c_int, _vp]),
     "pgb_mlp_f32_to_bf16": (C.c_int, [_vp, _vp, C.c_longlong, _vp]),
+    "pgb_mlp_dup_weight_bf16": (C.c_int, [_vp, C.c_int, C.c_int, _vp, C.c_int, _vp]),
+    "pgb_mlp_split_rows_bf16": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _vp, C.c_int, C.c_int, _vp]),
     "pgb_react_boxes_noalloc": (C.c_int, [C.c_char_p, C.POINTER(BoxView), C.c_int, C.c_double,
                                           C.c_double, C.c_double, C.c_int, C.c_int, C.c_int, _vp,
                                           C.POINTER(Stats)]),

@@ -127,6 +127,7 @@ __global__ void __launch_bounds__(TPB, 1) bdf_reactor_kernel(const ReactParams P
   // ---- per-lane state ----
   int phase = NEED;
   long long cell = -1;
+  const long long ncell = P.ncell_dev ? (long long)*P.ncell_dev : P.ncell;
   int box = 0, ci = 0, cj = 0, ck = 0;
   double y[N], acor[N], ewt[N];
   double t = 0.0, h = 0.0, hscale = 0.0, etamax = ETAMX1, eta = 1.0;
@@ -430,11 +431,11 @@ __global__ void __launch_bounds__(TPB, 1) bdf_reactor_kernel(const ReactParams P
       base = __shfl_sync(0xffffffffu, base, leader);
       if (phase == NEED) {
         const long long c = (long long)base + __popc(need & ((1u << lane) - 1u));
-        if (c >= P.ncell) {
+        if (c >= ncell) {
           phase = IDLE;
         } else {
-          cell = c;
-          if (load_cell(c)) phase = START;  // masked cells stay NEED and refetch next pass
+          cell = P.cell_list ? P.cell_list[c] : c;
+          if (load_cell(cell)) phase = START;  // masked cells stay NEED and refetch next pass
         }
       }
     }

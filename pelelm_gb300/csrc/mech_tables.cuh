@@ -147,7 +147,7 @@ __device__ void jac_table(const double* y, Frc Fr, double Fh, Acc J, Scr Cs) {
         dG -= g;
         dH -= h;
       }
-      kr = kf * pgb_expT<R>(dG);
+      kr = kf * pgb_expT<R>(fmin(dG, R(700)));  // finite: Pp = 0 gives 0, not NaN
       dlnkr = dlnkf - (dH - (R)r.dnu) * invT;
     }
     const R q = alpha * (kf * Pf - kr * Pp);
@@ -283,7 +283,7 @@ __device__ __forceinline__ void rhs_table(const double* y, Frc Fr, double Fh, do
       double dG = -r.dnu * lnP0RT;
       for (int s = 0; s < r.np; ++s) dG += Gs(r.ps[s]);
       for (int s = 0; s < r.nr; ++s) dG -= Gs(r.rs[s]);
-      const double kr = kf * pgb_exp64(dG);
+      const double kr = kf * pgb_exp64(fmin(dG, 700.0));  // finite: Pp = 0 gives 0, not NaN
       q = fma(kf, Pf, -kr * Pp);
     } else {
       q = kf * Pf;

@@ -15,47 +15,9 @@
 
 #include "reactor_registry.cuh"
 
+#include "mlp_common.cuh"
+
 namespace pgb_mlp {
-
-using bf16 = __nv_bfloat16;
-
-__device__ __forceinline__ unsigned smem_u32(const void* p) {
-  return static_cast<unsigned>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ void cp_async16(void* smem, const void* gmem, bool valid) {
-  const int n = valid ? 16 : 0;  // 0 source bytes => zero fill
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(smem_u32(smem)), "l"(gmem), "r"(n));
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
-
-__device__ __forceinline__ void ldmatrix_x4(unsigned& r0, unsigned& r1, unsigned& r2, unsigned& r3,
-                                            const void* p) {
-  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
-               : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
-               : "r"(smem_u32(p)));
-}
-
-__device__ __forceinline__ void mma_bf16(float* d, const unsigned* a, const unsigned* b) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-      "{%0,%1,%2,%3};\n"
-      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
-}
-
-__device__ __forceinline__ float gelu(float x) {  // tanh form
-  const float u = 0.7978845608028654f * (x + 0.044715f * x * x * x);
-  return 0.5f * x * (1.f + tanhf(u));
-}
-__device__ __forceinline__ float gelu_grad(float x) {
-  const float x2 = x * x;
-  const float u = 0.7978845608028654f * (x + 0.044715f * x2 * x);
-  const float t = tanhf(u);
-  return 0.5f * (1.f + t) + 0.5f * x * (1.f - t * t) * 0.7978845608028654f * (1.f + 3.f * 0.044715f * x2);
-}
 
 constexpr int BM = 128, BN = 128, BK = 32, PAD = 8, LDS = BK + PAD;  // shared row: 40 bf16 = 80 B
 
@@ -242,6 +204,33 @@ __global__ void f32_to_bf16_kernel(const float* __restrict__ in, bf16* __restric
     out[i] = __float2bfloat16(in[i]);
 }
 
+// Row r of W (rows x cols, FP32) -> BF16 twice, at out[r*ldo + c] and out[r*ldo + cols + c]: the
+// first-layer weight seen by an input split into high and low BF16 halves (split_rows_kernel).
+__global__ void dup_weight_kernel(const float* __restrict__ W, int rows, int cols, bf16* __restrict__ out,
+                                  int ldo) {
+  const long long n = (long long)rows * cols;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int r = (int)(i / cols), c = (int)(i % cols);
+    const bf16 w = __float2bfloat16(W[i]);
+    out[(long long)r * ldo + c] = w;
+    out[(long long)r * ldo + cols + c] = w;
+  }
+}
+
+// x (FP32) -> hi = bf16(x) at column c, lo = bf16(x - hi) at column off + c: with FP32 accumulation
+// the pair carries ~16 significant bits of x through a BF16 GEMM.
+__global__ void split_rows_kernel(const float* __restrict__ x, int rows, int cols, int ldx, bf16* __restrict__ out,
+                                  int ldo, int off) {
+  const long long n = (long long)rows * cols;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int r = (int)(i / cols), c = (int)(i % cols);
+    const float v = x[(long long)r * ldx + c];
+    const bf16 hi = __float2bfloat16(v);
+    out[(long long)r * ldo + c] = hi;
+    out[(long long)r * ldo + off + c] = __float2bfloat16(v - __bfloat162float(hi));
+  }
+}
+
 }  // namespace pgb_mlp
 
 using namespace pgb_host;
@@ -307,6 +296,24 @@ int pgb_mlp_adam(float* p, const float* g, float* m, float* v, void* p_bf16, lon
 int pgb_mlp_f32_to_bf16(const float* in, void* out, long long n, void* stream) {
   pgb_mlp::f32_to_bf16_kernel<<<grid_for(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(
       in, static_cast<bf16*>(out), n);
+  PGB_CUDA(cudaGetLastError());
+  return 0;
+}
+
+int pgb_mlp_dup_weight_bf16(const float* W, int rows, int cols, void* out, int ldo, void* stream) {
+  if (rows <= 0 || cols <= 0 || ldo < 2 * cols) return set_err("dup_weight: need ldo >= 2*cols");
+  pgb_mlp::dup_weight_kernel<<<grid_for((long long)rows * cols), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+      W, rows, cols, static_cast<bf16*>(out), ldo);
+  PGB_CUDA(cudaGetLastError());
+  return 0;
+}
+
+int pgb_mlp_split_rows_bf16(const float* x, int rows, int cols, int ldx, void* out, int ldo, int off,
+                            void* stream) {
+  if (rows <= 0 || cols <= 0 || off < cols || ldo < off + cols || ldx < cols)
+    return set_err("split_rows: need cols <= off and off + cols <= ldo");
+  pgb_mlp::split_rows_kernel<<<grid_for((long long)rows * cols), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+      x, rows, cols, ldx, static_cast<bf16*>(out), ldo, off);
   PGB_CUDA(cudaGetLastError());
   return 0;
 }

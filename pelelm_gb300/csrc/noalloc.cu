@@ -58,6 +58,7 @@ extern "C" int pgb_react_boxes_noalloc(const char* mechanism, const pgb_box_view
                                        int max_steps, int fp64, void* stream, pgb_stats* stats) {
   const MechEntry* m = find_mech_entry(mechanism);
   if (!m) return set_err("unknown mechanism '%s'", mechanism ? mechanism : "(null)");
+  if (!m->bdf_mixed) return set_err("noalloc: mechanism '%s' has no cell-per-thread kernel", m->name);
   if (nbox < 1 || !views) return set_err("noalloc: need at least one box view");
   if (nbox > PGB_NOALLOC_MAX_BOXES)
     return set_err("noalloc: %d boxes exceed the fixed scratch capacity of %d boxes; split the "
@@ -101,6 +102,8 @@ extern "C" int pgb_react_boxes_noalloc(const char* mechanism, const pgb_box_view
   p.stats = &S->stats;
   p.lu_scratch = nullptr;  // Jacobian/LU slices and Nordsieck histories stay in shared memory
   p.z_scratch = nullptr;
+  p.cell_list = nullptr;
+  p.ncell_dev = nullptr;
   int dev = 0, nsm = 0;
   PGB_CUDA(cudaGetDevice(&dev));
   PGB_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));

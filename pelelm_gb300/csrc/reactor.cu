@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "reactor_registry.cuh"
+#include "surrogate_host.h"
 
 namespace pgb_host {
 
@@ -37,6 +38,7 @@ int set_err(const char* fmt, ...) {
 
 extern const MechEntry kEntry_lidryer_syn;
 extern const MechEntry kEntry_drm19_syn;
+extern const MechEntry kEntry_gri_syn;
 
 }  // namespace pgb_host
 
@@ -56,8 +58,13 @@ struct Options {
   bool graph = false;
   int z_global = -1;       // gb.history = shared | global (L2-resident Nordsieck); -1 = auto
   int lu_global = -1;      // gb.lu = shared | global (L2-resident Jacobian/LU); -1 = auto
+  int mapping = -1;        // gb.mapping = thread (cell per thread) | warp (cell per warp); -1 = auto
+  int wpb = 0;             // gb.wpb: warps per block of the warp mapping (0 = most that fit)
   std::string solve_type = "denseAJ_direct";
   int analytical_jacobian = 1;
+  std::string surrogate;   // gb.surrogate = trained surrogate file: surrogate + BDF fallback
+  SgOverrides sg;          // gb.sg.* threshold overrides
+  unsigned long long sg_seed = 1;
 };
 
 int parse_options(const char* s, Options& o) {
@@ -85,6 +92,23 @@ int parse_options(const char* s, Options& o) {
         else return set_err("gb.precision must be mixed or fp64, got '%s'", v.c_str());
       } else if (k == "gb.tpb") o.tpb = std::stoi(v);
       else if (k == "gb.graph") o.graph = std::stoi(v) != 0;
+      else if (k == "gb.mapping") {
+        if (v == "thread") o.mapping = 0;
+        else if (v == "warp") o.mapping = 1;
+        else return set_err("gb.mapping must be thread or warp, got '%s'", v.c_str());
+      } else if (k == "gb.wpb") o.wpb = std::stoi(v);
+      else if (k == "gb.surrogate") o.surrogate = v;
+      else if (k == "gb.sg.audit") o.sg.audit_frac = std::stod(v);
+      else if (k == "gb.sg.mis") o.sg.mis = std::stod(v);
+      else if (k == "gb.sg.cons") o.sg.cons = std::stod(v);
+      else if (k == "gb.sg.disT") o.sg.disT = std::stod(v);
+      else if (k == "gb.sg.disY") o.sg.disY = std::stod(v);
+      else if (k == "gb.sg.neg") o.sg.neg = std::stod(v);
+      else if (k == "gb.sg.ood_margin") o.sg.ood_margin = std::stod(v);
+      else if (k == "gb.sg.tol_T") o.sg.tol_T = std::stod(v);
+      else if (k == "gb.sg.tol_Y") o.sg.tol_Y = std::stod(v);
+      else if (k == "gb.sg.models") o.sg.models = std::stoi(v);
+      else if (k == "gb.sg.seed") o.sg_seed = std::stoull(v);
       else if (k == "gb.history" || k == "gb.lu") {
         int& f = (k == "gb.history") ? o.z_global : o.lu_global;
         if (v == "global") f = 1;
@@ -156,6 +180,13 @@ struct Scratch {
   void* d_lu = nullptr;            // Jacobian/LU slices of the resident threads
   size_t lu_cap = 0;
   pgb::ReactStats* d_stats = nullptr;
+  // surrogate: fallback cell list, audit records, counters
+  void* d_fallback = nullptr;
+  size_t fallback_cap = 0;
+  void* d_audit = nullptr;
+  size_t audit_cap = 0;
+  unsigned long long* d_sg_counts = nullptr;  // fallback count, audit count, seed
+  pgb::SurrogateStats* d_sg_stats = nullptr;
   cudaEvent_t done = nullptr;
   long long last_ncell = 0;
   // graph cache
@@ -176,6 +207,7 @@ struct pgb_reactor {
   std::map<cudaStream_t, Scratch> scratch;
   cudaStream_t last_stream = nullptr;
   int device = 0, nsm = 0;
+  SgModel sg;  // loaded when options name a surrogate file
 };
 
 namespace {
@@ -188,6 +220,10 @@ void free_scratch(Scratch& s) {
   if (s.d_stats) cudaFree(s.d_stats);
   if (s.d_z) cudaFree(s.d_z);
   if (s.d_lu) cudaFree(s.d_lu);
+  if (s.d_fallback) cudaFree(s.d_fallback);
+  if (s.d_audit) cudaFree(s.d_audit);
+  if (s.d_sg_counts) cudaFree(s.d_sg_counts);
+  if (s.d_sg_stats) cudaFree(s.d_sg_stats);
   if (s.done) cudaEventDestroy(s.done);
   s = Scratch();
 }
@@ -198,6 +234,12 @@ int ensure_scratch(pgb_reactor* r, cudaStream_t st, size_t nbox, Scratch** out) 
     PGB_CUDA(cudaMalloc(&s.d_counter, sizeof(unsigned long long)));
     PGB_CUDA(cudaMalloc(&s.d_stats, sizeof(pgb::ReactStats)));
     PGB_CUDA(cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming));
+    if (r->sg.d_net) {
+      PGB_CUDA(cudaMalloc(&s.d_sg_counts, 3 * sizeof(unsigned long long)));
+      PGB_CUDA(cudaMalloc(&s.d_sg_stats, sizeof(pgb::SurrogateStats)));
+      const unsigned long long seed = r->opt.sg_seed;
+      PGB_CUDA(cudaMemcpy(s.d_sg_counts + 2, &seed, sizeof(seed), cudaMemcpyHostToDevice));
+    }
   }
   if (nbox > s.box_cap) {
     if (s.done) PGB_CUDA(cudaEventSynchronize(s.done));
@@ -223,7 +265,10 @@ struct LaunchPlan {
   int tpb = 128, nblocks = 1;
   bool z_global = false, lu_global = false;
   size_t z_bytes = 0, lu_bytes = 0;
+  bool warp = false;  // warp-per-cell kernel; tpb then holds warps per block
 };
+
+bool use_warp(const pgb_reactor* r);
 
 // First layout (all shared; global Nordsieck history; global history and LU) whose shared
 // footprint fits 128 threads per block (the occupancy that measures best), unless options
@@ -231,6 +276,20 @@ struct LaunchPlan {
 LaunchPlan plan_launch(const pgb_reactor* r, long long ncell) {
   LaunchPlan pl;
   const MechEntry& m = *r->mech;
+  if (use_warp(r)) {
+    // warp per cell: as many warps per block as fit shared memory (or gb.wpb), one block per SM
+    const int per = r->opt.mixed ? m.wsmem_mixed : m.wsmem_fp64;
+    int wpb = r->opt.wpb;
+    if (wpb <= 0) {
+      wpb = 4;
+      for (int c : {16, 8, 6})
+        if (c * per <= kMaxSmemPerBlock) { wpb = c; break; }
+    }
+    pl.warp = true;
+    pl.tpb = wpb;
+    pl.nblocks = (int)std::min<long long>(r->nsm, std::max<long long>(1, (ncell + wpb - 1) / wpb));
+    return pl;
+  }
   const int per[3] = {r->opt.mixed ? m.smem_mixed : m.smem_fp64, r->opt.mixed ? m.smem_mixed_g : m.smem_fp64_g,
                       r->opt.mixed ? m.smem_mixed_gl : m.smem_fp64_gl};
   const int tpb = r->opt.tpb > 0 ? r->opt.tpb : 128;
@@ -269,6 +328,20 @@ int ensure_buf(Scratch& s, void*& buf, size_t& cap, size_t bytes) {
   return 0;
 }
 
+// Cell-per-thread kernels exist for mechanisms whose per-cell state fits a thread; the others
+// (and gb.mapping=warp) take the warp-per-cell kernel.
+bool use_warp(const pgb_reactor* r) {
+  if (!r->mech->bdf_mixed) return true;
+  return r->opt.mapping == 1;
+}
+
+// Audit records kept per call: twice the expected sample plus slack (cells past the capacity
+// are simply not audited).
+long long audit_capacity(const pgb_reactor* r, long long ncell) {
+  if (!(r->sg.audit_frac > 0.0)) return 0;
+  return std::min<long long>(ncell, (long long)(2.0 * r->sg.audit_frac * (double)ncell) + 1024);
+}
+
 int enqueue_advance(pgb_reactor* r, Scratch& s, int nbox, long long ncell, double dt,
                     cudaStream_t st) {
   pgb::ReactParams p;
@@ -296,8 +369,34 @@ int enqueue_advance(pgb_reactor* r, Scratch& s, int nbox, long long ncell, doubl
   const LaunchPlan pl = plan_launch(r, ncell);
   p.lu_scratch = pl.lu_bytes ? s.d_lu : nullptr;
   p.z_scratch = pl.z_bytes ? s.d_z : nullptr;
-  LaunchFn fn = r->opt.mixed ? r->mech->bdf_mixed : r->mech->bdf_fp64;
-  return fn(p, pl.tpb, st, pl.nblocks);
+  LaunchFn fn = pl.warp ? (r->opt.mixed ? r->mech->warp_mixed : r->mech->warp_fp64)
+                        : (r->opt.mixed ? r->mech->bdf_mixed : r->mech->bdf_fp64);
+  if (!r->sg.d_net) return fn(p, pl.tpb, st, pl.nblocks);
+
+  // surrogate for every cell; the cells it does not accept (and the audit sample) go to the
+  // BDF through the device list, then the audit compares
+  pgb::SurrogateParams sp;
+  sp.boxes = s.d_boxes;
+  sp.nbox = nbox;
+  sp.ncell = ncell;
+  sp.dt = dt;
+  sp.net = r->sg.d_net;
+  sp.fallback_list = static_cast<long long*>(s.d_fallback);
+  sp.fallback_count = s.d_sg_counts;
+  sp.audit_count = s.d_sg_counts + 1;
+  sp.seed_dev = s.d_sg_counts + 2;
+  sp.audit_cap = audit_capacity(r, ncell);
+  sp.audit_cell = static_cast<long long*>(s.d_audit);
+  sp.audit_pred = reinterpret_cast<double*>(static_cast<long long*>(s.d_audit) + sp.audit_cap);
+  sp.stats = s.d_sg_stats;
+  PGB_CUDA(cudaMemsetAsync(s.d_sg_counts, 0, 2 * sizeof(unsigned long long), st));
+  PGB_CUDA(cudaMemsetAsync(s.d_sg_stats, 0, sizeof(pgb::SurrogateStats), st));
+  const long long ntiles = (ncell + pgb::SG_TILE - 1) / pgb::SG_TILE;
+  if (r->mech->sg_fn(sp, st, (int)std::min<long long>(ntiles, r->nsm))) return -1;
+  p.cell_list = sp.fallback_list;
+  p.ncell_dev = sp.fallback_count;
+  if (fn(p, pl.tpb, st, pl.nblocks)) return -1;
+  return r->mech->sg_audit_fn(sp, st, r->nsm);
 }
 
 }  // namespace
@@ -346,6 +445,14 @@ pgb_reactor* pgb_reactor_create(const char* name, const char* mechanism, int rea
   }
   Options o;
   if (parse_options(options, o)) return nullptr;
+  if (o.mapping == 0 && !m->bdf_mixed) {
+    set_err("mechanism '%s' has no cell-per-thread kernel (gb.mapping=warp)", m->name);
+    return nullptr;
+  }
+  if (!o.surrogate.empty() && !m->sg_fn) {
+    set_err("no surrogate kernel is compiled for mechanism '%s'", m->name);
+    return nullptr;
+  }
   int dev = 0, nsm = 0;
   if (cudaGetDevice(&dev) != cudaSuccess ||
       cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
@@ -359,6 +466,13 @@ pgb_reactor* pgb_reactor_create(const char* name, const char* mechanism, int rea
   r->null_reactor = (n == "ReactorNull");
   r->device = dev;
   r->nsm = nsm;
+  if (!o.surrogate.empty()) {
+    if (r->null_reactor || sg_load(o.surrogate.c_str(), m->name, m->ns, o.sg, r->sg)) {
+      if (r->null_reactor) set_err("gb.surrogate needs ReactorCvode (its fallback integrator)");
+      delete r;
+      return nullptr;
+    }
+  }
   return r;
 }
 
@@ -389,6 +503,13 @@ int pgb_reactor_react_boxes(pgb_reactor* r, const pgb_box_view* views, int nbox,
     const LaunchPlan pl = plan_launch(r, ncell);
     if (ensure_buf(*s, s->d_z, s->z_cap, pl.z_bytes) || ensure_buf(*s, s->d_lu, s->lu_cap, pl.lu_bytes))
       return -1;
+    if (r->sg.d_net) {
+      const long long acap = audit_capacity(r, ncell);
+      if (ensure_buf(*s, s->d_fallback, s->fallback_cap, std::max<long long>(ncell, 1) * sizeof(long long)) ||
+          ensure_buf(*s, s->d_audit, s->audit_cap,
+                     std::max<long long>(acap, 1) * (sizeof(long long) + pgb::MAXN * sizeof(double))))
+        return -1;
+    }
   }
   PGB_CUDA(cudaEventSynchronize(s->done));  // staging buffer may still feed a previous copy
   if (nbox) std::memcpy(s->h_boxes, boxes.data(), nbox * sizeof(pgb::BoxDev));
@@ -432,6 +553,24 @@ int pgb_reactor_get_stats(pgb_reactor* r, pgb_stats* out) {
   return 0;
 }
 
+int pgb_reactor_get_surrogate_stats(pgb_reactor* r, pgb_surrogate_stats* out) {
+  if (!r || !out) return set_err("null argument");
+  if (!r->sg.d_net) return set_err("reactor has no surrogate (gb.surrogate)");
+  std::lock_guard<std::mutex> g(r->mu);
+  auto it = r->scratch.find(r->last_stream);
+  if (it == r->scratch.end()) return set_err("no advance has run yet");
+  Scratch& s = it->second;
+  pgb::SurrogateStats h;
+  PGB_CUDA(cudaEventSynchronize(s.done));
+  PGB_CUDA(cudaMemcpy(&h, s.d_sg_stats, sizeof(h), cudaMemcpyDeviceToHost));
+  out->ncell = h.ncell; out->accept = h.accept; out->fallback = h.fallback;
+  out->ood = h.ood; out->mis = h.mis; out->cons = h.cons; out->ens = h.ens; out->neg = h.neg;
+  out->audit = h.audit; out->audit_bad = h.audit_bad;
+  std::memcpy(&out->audit_max_dT, &h.audit_max_dT, sizeof(double));
+  std::memcpy(&out->audit_max_dY, &h.audit_max_dY, sizeof(double));
+  return 0;
+}
+
 int pgb_reactor_react(pgb_reactor* r, const pgb_box_view* view, double* dt_react, double* time,
                       void* stream) {
   if (!r || !view || !dt_react || !time) return set_err("null argument");
@@ -449,6 +588,7 @@ void pgb_reactor_close(pgb_reactor* r) {
       if (kv.second.done) cudaEventSynchronize(kv.second.done);
       free_scratch(kv.second);
     }
+    sg_free(r->sg);
   }
   delete r;
 }
@@ -458,6 +598,7 @@ int pgb_reaction_rates(const char* mechanism, const pgb_box_view* view, const pg
   const MechEntry* m = find_mech(mechanism);
   if (!m) return set_err("unknown mechanism '%s'", mechanism ? mechanism : "(null)");
   if (!view || !out) return set_err("null argument");
+  if (!m->rates_fn) return set_err("pointwise rates are not compiled for mechanism '%s'", m->name);
   return m->rates_fn(view, out, static_cast<cudaStream_t>(stream));
 }
 
@@ -474,7 +615,7 @@ int pgb_rhoh_to_temp(const char* mechanism, const pgb_box_view* view, double tmi
 
 namespace {
 
-const MechEntry* const kMechs[] = {&kEntry_lidryer_syn, &kEntry_drm19_syn};
+const MechEntry* const kMechs[] = {&kEntry_lidryer_syn, &kEntry_drm19_syn, &kEntry_gri_syn};
 
 const MechEntry* find_mech(const char* name) {
   if (!name) return nullptr;

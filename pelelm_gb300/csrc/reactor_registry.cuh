@@ -7,8 +7,10 @@
 
 #include "../../include/pelelm_gb300.h"
 #include "bdf_kernel.cuh"
+#include "bdf_warp_kernel.cuh"
 #include "point_kernels.cuh"
 #include "reactor_types.cuh"
+#include "surrogate_kernel.cuh"
 
 namespace pgb_host {
 
@@ -68,9 +70,54 @@ int launch_bdf(const pgb::ReactParams& p, int tpb, cudaStream_t s, int nblocks) 
   }
 }
 
+// Warp-per-cell BDF: `wpb` warps per block (4, 6, 8 or 16), one persistent block per SM.
+template <class M, class JR, int WPB>
+int launch_bdf_warp_wpb(const pgb::ReactParams& p, cudaStream_t s, int nblocks) {
+  constexpr int smem = WPB * pgb::bdf_warp_smem_per_warp<M, JR>();
+  if constexpr (smem > kMaxSmemPerBlock) {
+    return set_err("warp BDF: %d warps x %d B shared memory exceed the %d B per block", WPB,
+                   pgb::bdf_warp_smem_per_warp<M, JR>(), kMaxSmemPerBlock);
+  } else {
+    auto kern = pgb::bdf_warp_kernel<M, JR, WPB>;
+    PGB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    kern<<<nblocks, WPB * 32, smem, s>>>(p);
+    PGB_CUDA(cudaGetLastError());
+    return 0;
+  }
+}
+
+template <class M, class JR>
+int launch_bdf_warp(const pgb::ReactParams& p, int wpb, cudaStream_t s, int nblocks) {
+  switch (wpb) {
+    case 4: return launch_bdf_warp_wpb<M, JR, 4>(p, s, nblocks);
+    case 6: return launch_bdf_warp_wpb<M, JR, 6>(p, s, nblocks);
+    case 8: return launch_bdf_warp_wpb<M, JR, 8>(p, s, nblocks);
+    case 16: return launch_bdf_warp_wpb<M, JR, 16>(p, s, nblocks);
+    default: return set_err("warp BDF: gb.wpb must be 4, 6, 8 or 16 (got %d)", wpb);
+  }
+}
+
 template <class M>
 int launch_null(const pgb::ReactParams& p, cudaStream_t s, int nblocks) {
   pgb::null_reactor_kernel<M><<<nblocks, 256, 0, s>>>(p);
+  PGB_CUDA(cudaGetLastError());
+  return 0;
+}
+
+template <class M>
+int launch_surrogate(const pgb::SurrogateParams& p, cudaStream_t s, int nblocks) {
+  constexpr int smem = (int)pgb::sg_smem_bytes();
+  static_assert(smem <= kMaxSmemPerBlock, "surrogate tile does not fit shared memory");
+  auto kern = pgb::surrogate_kernel<M>;
+  PGB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  kern<<<nblocks, 256, smem, s>>>(p);
+  PGB_CUDA(cudaGetLastError());
+  return 0;
+}
+
+template <class M>
+int launch_surrogate_audit(const pgb::SurrogateParams& p, cudaStream_t s, int nblocks) {
+  pgb::surrogate_audit_kernel<M><<<nblocks, 256, 0, s>>>(p);
   PGB_CUDA(cudaGetLastError());
   return 0;
 }
@@ -85,6 +132,10 @@ struct MechEntry {
   int smem_mixed_gl, smem_fp64_gl;  // shared bytes per thread, history and LU in global scratch
   int (*rates_fn)(const pgb_box_view*, const pgb_array4*, cudaStream_t);
   int (*h2t_fn)(const pgb_box_view*, double, double, cudaStream_t);
+  int (*sg_fn)(const pgb::SurrogateParams&, cudaStream_t, int);
+  int (*sg_audit_fn)(const pgb::SurrogateParams&, cudaStream_t, int);
+  LaunchFn warp_mixed, warp_fp64;  // warp-per-cell BDF (argument: warps per block)
+  int wsmem_mixed, wsmem_fp64;     // shared bytes per warp
 };
 
 
@@ -159,7 +210,19 @@ int h2t_entry(const pgb_box_view* v, double tmin, double tmax, cudaStream_t s) {
         pgb::bdf_smem_per_thread<M, double, pgb::LAYOUT_Z_GLOBAL>(),                         \
         pgb::bdf_smem_per_thread<M, float, 3>(), pgb::bdf_smem_per_thread<M, double, 3>(),   \
         ::pgb_host::rates_entry<M>,                                                          \
-        ::pgb_host::h2t_entry<M>                                                             \
+        ::pgb_host::h2t_entry<M>, ::pgb_host::launch_surrogate<M>,                           \
+        ::pgb_host::launch_surrogate_audit<M>, ::pgb_host::launch_bdf_warp<M, float>,        \
+        ::pgb_host::launch_bdf_warp<M, double>, pgb::bdf_warp_smem_per_warp<M, float>(),     \
+        pgb::bdf_warp_smem_per_warp<M, double>()                                             \
+  }
+
+// Mechanisms too large for one cell per thread: warp-per-cell BDF, ReactorNull and T(h, Y) only.
+#define PGB_MECH_ENTRY_WARP(M)                                                               \
+  ::pgb_host::MechEntry {                                                                    \
+    M::NAME, M::NS, M::NR, nullptr, nullptr, ::pgb_host::launch_null<M>, 0, 0, 0, 0, 0, 0,    \
+        nullptr, ::pgb_host::h2t_entry<M>, nullptr, nullptr,                                 \
+        ::pgb_host::launch_bdf_warp<M, float>, ::pgb_host::launch_bdf_warp<M, double>,       \
+        pgb::bdf_warp_smem_per_warp<M, float>(), pgb::bdf_warp_smem_per_warp<M, double>()    \
   }
 
 // Converts and validates one box view into its device descriptor; cell numbering of the box

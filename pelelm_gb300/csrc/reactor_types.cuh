@@ -53,6 +53,11 @@ struct ReactParams {
   ReactStats* stats;              // device scratch
   void* lu_scratch;               // per-thread Jacobian/LU slices in global memory, or null
   void* z_scratch;                // per-thread Nordsieck histories in global memory, or null
+  // Optional indirection (both null for a plain advance): queue entry c < *ncell_dev advances
+  // flat cell cell_list[c]. Lets a producer kernel on the same stream hand over a cell subset
+  // (the surrogate's fallback cells) without a host round trip.
+  const long long* cell_list;
+  const unsigned long long* ncell_dev;
 };
 
 }  // namespace pgb

@@ -100,12 +100,16 @@ def gen_header(m: Mechanism) -> str:
     e(f"#ifndef {guard}")
     e(f"#define {guard}")
     e('#include "../mech_common.cuh"')
-    e(f'#include "tab_{m.name}.cuh"')
+    const_tab = m.name in CONSTANT_TABLES
+    if const_tab:
+        e(f'#include "tab_{m.name}.cuh"')
+    e(f'#include "tabg_{m.name}.cuh"')
     e()
     e("namespace pgb {")
     e(f"struct Mech_{m.name} {{")
     e.ind += 1
-    e(f"using Tab = tab_{m.name}::Tables;")
+    e(f"using Tab = {'tab' if const_tab else 'tabg'}_{m.name}::Tables;  // per-thread kernels")
+    e(f"using TabG = tabg_{m.name}::Tables;  // warp-per-cell kernel")
     e(f"static constexpr int NS = {ns};")
     e(f"static constexpr int NR = {nr};")
     e(f"static constexpr int N = {N};")
@@ -194,7 +198,9 @@ def gen_header(m: Mechanism) -> str:
                 dgs = " ".join(dg).lstrip("+ ").strip()
                 if dnu != 0:
                     dgs += f" - {_f(dnu)} * lnP0RT"
-                e(f"const double kr = kf * pgb_exp({dgs});")
+                # exponent capped at 700: exp stays finite, so an absent product (Pp = 0)
+                # gives a zero reverse term instead of inf * 0 = NaN
+                e(f"const double kr = kf * pgb_exp(fmin({dgs}, 700.0));")
                 e(f"q{j} = fma(kf, {pf}, -kr * {pr});")
             else:
                 e(f"q{j} = kf * {pf};")
@@ -355,7 +361,7 @@ def gen_header(m: Mechanism) -> str:
             dgs = " ".join(dg)
             if dnu != 0:
                 dgs += f" - R({dnu}) * lnP0RT"
-            e(f"const R kr = kf * pgb_expT<R>(R(0) {dgs});")
+            e(f"const R kr = kf * pgb_expT<R>(fmin(R(0) {dgs}, R(700)));")
             e(f"const R dlnkr = dlnkf - (R(0) {' '.join(dh)} - R({dnu})) * invT;")
         else:
             e("const R kr = R(0);")
@@ -453,11 +459,20 @@ if __name__ == "__main__":
 
 
 # ---------------------------------------------------------------------------- tables
-def gen_tables(m: Mechanism) -> str:
-    """Constant-memory tables of a mechanism for the table-driven Jacobian (and any other
-    loop-over-reactions kernel): per-species W, NASA-7 sets, per-reaction Arrhenius data,
-    stoichiometry as species slots (a species with coefficient 2 occupies two slots), sparse
-    third-body efficiencies and Troe parameters."""
+def gen_tables(m: Mechanism, space: str = "constant") -> str:
+    """Mechanism tables for the table-driven kernels: per-species W, NASA-7 sets, per-reaction
+    Arrhenius data, stoichiometry as species slots (a species with coefficient 2 occupies two
+    slots), sparse third-body efficiencies and Troe parameters.
+
+    space "constant": __constant__ arrays in namespace tab_<name> (per-thread kernels: every lane
+    reads the same entry, a constant-cache broadcast). space "global": read-only global arrays in
+    namespace tabg_<name> (warp-per-cell kernels: lanes read different entries through L1; also
+    the only choice when the tables exceed the 64 KB constant bank), plus the species-major list
+    of the reactions each species takes part in with its net coefficient (production rates as a
+    gather)."""
+    glob = space == "global"
+    qual = "__device__ const" if glob else "__device__ __constant__"
+    nsname = f"tabg_{m.name}" if glob else f"tab_{m.name}"
     ns = m.ns
     idx = {s.name: i for i, s in enumerate(m.species)}
     tb_rows, troe_rows = [], []
@@ -486,16 +501,16 @@ def gen_tables(m: Mechanism) -> str:
                    rs, ps, dnu, tb, tr))
     maxeff = max([len(t) for t in tb_rows] + [1])
     e = _Emitter()
-    e(f"// GENERATED by pelelm_gb300/mech/codegen.py (tables) from pelelm_gb300/data/{m.name}.json.")
-    guard = f"PGB_TAB_{m.name.upper()}_CUH"
+    e(f"// GENERATED by pelelm_gb300/mech/codegen.py (tables, {space} memory) from pelelm_gb300/data/{m.name}.json.")
+    guard = f"PGB_{nsname.upper()}_CUH"
     e(f"#ifndef {guard}")
     e(f"#define {guard}")
     e('#include "../mech_tables.cuh"')
     e("namespace pgb {")
-    e(f"namespace tab_{m.name} {{")
+    e(f"namespace {nsname} {{")
     e(f"constexpr int NS = {ns}, NR = {m.nr}, NTB = {max(1, len(tb_rows))}, NTROE = {max(1, len(troe_rows))}, MAXEFF = {maxeff};")
     for R, suf, cast in (("double", "D", lambda x: _f(x)), ("float", "F", lambda x: _f(x) + "f")):
-        e(f"__device__ __constant__ TabSpecies<{R}> kSpecies{suf}[NS] = {{")
+        e(f"{qual} TabSpecies<{R}> kSpecies{suf}[NS] = {{")
         def gco(a):
             return [a[0], -a[1] / 2, -a[2] / 6, -a[3] / 12, -a[4] / 20, a[5], -a[6]]
 
@@ -507,13 +522,13 @@ def gen_tables(m: Mechanism) -> str:
             body = ", ".join("{" + ", ".join(cast(a_) for a_ in arr) + "}" for arr in arrs)
             e(f"  {{{cast(sp_.W)}, {cast(1.0 / sp_.W)}, {cast(sp_.Tmid)}, {body}}},")
         e("};")
-        e(f"__device__ __constant__ TabReaction<{R}> kReactions{suf}[NR] = {{")
+        e(f"{qual} TabReaction<{R}> kReactions{suf}[NR] = {{")
         for (lnA, beta, mear, kind, rev, rs, ps, dnu, tb, tr) in rx:
             rsl = ", ".join(str(x) for x in (rs + [0, 0, 0])[:3])
             psl = ", ".join(str(x) for x in (ps + [0, 0, 0])[:3])
             e(f"  {{{cast(lnA)}, {cast(beta)}, {cast(mear)}, {kind}, {rev}, {len(rs)}, {len(ps)}, {{{rsl}}}, {{{psl}}}, {dnu}, {tb}, {tr}}},")
         e("};")
-        e(f"__device__ __constant__ TabThirdBody<{R}> kThirdBody{suf}[NTB] = {{")
+        e(f"{qual} TabThirdBody<{R}> kThirdBody{suf}[NTB] = {{")
         if not tb_rows:
             e(f"  {{0, {{0}}, {{{cast(0.0)}}}}},")
         for effs in tb_rows:
@@ -521,34 +536,64 @@ def gen_tables(m: Mechanism) -> str:
             ev = ", ".join(cast(v) for _, v in effs) or cast(0.0)
             e(f"  {{{len(effs)}, {{{sp}}}, {{{ev}}}}},")
         e("};")
-        e(f"__device__ __constant__ TabTroe<{R}> kTroe{suf}[NTROE] = {{")
+        e(f"{qual} TabTroe<{R}> kTroe{suf}[NTROE] = {{")
         if not troe_rows:
             e("  {" + ", ".join([cast(0.0)] * 3 + ["0"] + [cast(0.0)] * 5) + "},")
         for t in troe_rows:
             e("  {" + ", ".join(cast(v) if isinstance(v, float) else str(v) for v in t) + "},")
         e("};")
+    if glob:
+        # species-major reaction lists: species k takes part in reactions kSpRxJ[kSpRxOff[k]..
+        # kSpRxOff[k+1]) with net molar coefficient kSpRxNu (products minus reactants), in
+        # reaction order
+        off, jj, nu = [0], [], []
+        for k in range(ns):
+            for j, (_, _, _, _, _, rs_, ps_, _, _, _) in enumerate(rx):
+                net = ps_.count(k) - rs_.count(k)
+                if net != 0:
+                    jj.append(j)
+                    nu.append(float(net))
+            off.append(len(jj))
+        e(f"constexpr int NSPRX = {len(jj)};")
+        e(f"{qual} int kSpRxOff[NS + 1] = {{{', '.join(str(x) for x in off)}}};")
+        e(f"{qual} int kSpRxJ[NSPRX] = {{{', '.join(str(x) for x in jj)}}};")
+        e(f"{qual} double kSpRxNu[NSPRX] = {{{', '.join(_f(x) for x in nu)}}};")
     e("struct Tables {")
     e(f"  static constexpr int NS = {ns}, NR = {m.nr};")
+    if glob:
+        e("  __device__ static int sprx_begin(int k) { return kSpRxOff[k]; }")
+        e("  __device__ static int sprx_end(int k) { return kSpRxOff[k + 1]; }")
+        e("  __device__ static int sprx_j(int e) { return kSpRxJ[e]; }")
+        e("  __device__ static double sprx_nu(int e) { return kSpRxNu[e]; }")
     for nm, typ, arr in (("sp", "TabSpecies", "kSpecies"), ("rx", "TabReaction", "kReactions"),
                          ("tb", "TabThirdBody", "kThirdBody"), ("troe", "TabTroe", "kTroe")):
         e(f"  template <class R> __device__ static const {typ}<R>& {nm}(int i) {{")
         e(f"    if constexpr (sizeof(R) == sizeof(double)) return {arr}D[i]; else return {arr}F[i];")
         e("  }")
     e("};")
-    e(f"}}  // namespace tab_{m.name}")
+    e(f"}}  // namespace {nsname}")
     e("}  // namespace pgb")
     e(f"#endif  // {guard}")
     return e.text()
 
 
-def write_tables(outdir: str, names=("lidryer_syn", "drm19_syn")):
+# mechanisms whose tables fit the 64 KB constant bank (per-thread kernels); every mechanism
+# also gets the global-memory tables of the warp-per-cell kernel
+CONSTANT_TABLES = ("lidryer_syn", "drm19_syn")
+
+
+def write_tables(outdir: str, names=("lidryer_syn", "drm19_syn", "gri_syn")):
     from ..workloads import load_mechanism
     for n in names:
-        text = gen_tables(load_mechanism(n))
-        path = os.path.join(outdir, f"tab_{n}.cuh")
-        if os.path.exists(path):
-            with open(path) as f:
-                if f.read() == text:
-                    continue
-        with open(path, "w") as f:
-            f.write(text)
+        m = load_mechanism(n)
+        outs = [(f"tabg_{n}.cuh", gen_tables(m, "global"))]
+        if n in CONSTANT_TABLES:
+            outs.append((f"tab_{n}.cuh", gen_tables(m, "constant")))
+        for fname, text in outs:
+            path = os.path.join(outdir, fname)
+            if os.path.exists(path):
+                with open(path) as f:
+                    if f.read() == text:
+                        continue
+            with open(path, "w") as f:
+                f.write(text)

@@ -39,7 +39,10 @@ INERT = {"N2", "AR"}
 SHAPES = {
     "lidryer_syn": dict(species=LIDRYER_SPECIES, n_elem=14, n_tb=5, n_fo=2, n_irr=0, seed=11),
     "drm19_syn": dict(species=DRM19_SPECIES, n_elem=61, n_tb=12, n_fo=11, n_irr=2, seed=24),
-    "gri_syn": dict(species=None, n_elem=284, n_tb=12, n_fo=29, n_irr=4, seed=44),
+    # recomb_max_dh_kcal: recombination candidates must release at least this much (bond
+    # formation); the enumerated GRI-sized species set otherwise admits endothermic adducts
+    # whose decomposition runs at ~1e85 /s near 300 K
+    "gri_syn": dict(species=None, n_elem=284, n_tb=12, n_fo=29, n_irr=4, seed=44, recomb_max_dh_kcal=-20.0),
 }
 
 EFF_RANGES = {"H2O": (5.0, 12.0), "H2": (1.5, 2.5), "CO2": (2.0, 3.8), "CO": (1.4, 2.0),
@@ -51,7 +54,8 @@ def _formula_key(comp: Dict[str, int]) -> Tuple:
 
 
 def gri_species(rng: np.random.Generator) -> List[str]:
-    """drm19 list + 32 enumerated CcHhOoNn formulas (c<=3, h<=8, o<=2, n<=1)."""
+    """drm19 list + 32 enumerated CcHhOoNn formulas (c<=3, h<=8, o<=2, n<=1) at or below the
+    saturation limit H <= 2C + N + 2."""
     from .thermo_model import skeleton
     have = {_formula_key(parse_formula(s)) for s in DRM19_SPECIES}
     cands = []
@@ -61,6 +65,8 @@ def gri_species(rng: np.random.Generator) -> List[str]:
             continue
         heavy = c + o + n
         if heavy == 0:
+            continue
+        if h > 2 * c + n + 2:  # above the saturation limit: no such molecule
             continue
         _, unpaired = skeleton(comp)
         if unpaired > 2:
@@ -160,6 +166,9 @@ def generate(name: str, seed: int = None) -> Mechanism:
                 elements.append(e)
 
     recomb, transfer = enumerate_candidates(names)
+    if shape.get("recomb_max_dh_kcal") is not None:
+        lim = shape["recomb_max_dh_kcal"] * 1000.0 / R_CAL  # R*K
+        recomb = [c for c in recomb if _dH298(sp, c[0], c[1]) < lim]
 
     def score_transfer(lhs, rhs):
         dh = abs(_dH298(sp, lhs, rhs)) * 8.314e-3  # kJ/mol

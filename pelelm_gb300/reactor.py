@@ -122,6 +122,12 @@ class ReactorGB:
         return {"ncell": s.ncell, "nst": s.nst, "nfe": s.nfe, "nje": s.nje, "netf": s.netf,
                 "ncfn": s.ncfn, "nfail": s.nfail, "max_nst": s.max_nst, "hist": list(s.hist)}
 
+    def surrogate_stats(self) -> dict:
+        """Counters of the learned surrogate in the last advance (reactor made with gb.surrogate)."""
+        s = _lib.SurrogateStats()
+        check(lib().pgb_reactor_get_surrogate_stats(self._h, C.byref(s)), "get_surrogate_stats")
+        return {n: getattr(s, n) for n, _ in _lib.SurrogateStats._fields_}
+
     def close(self) -> None:
         if self._h:
             lib().pgb_reactor_close(self._h)

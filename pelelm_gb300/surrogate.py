@@ -43,10 +43,15 @@ class Normalizer:
 class SurrogateMLP:
     """MLP n_in -> width x depth (GELU) -> n_out with padded BF16 GEMMs on the GPU."""
 
-    def __init__(self, torch, n_in: int, n_out: int, width: int = 256, depth: int = 4, seed: int = 0):
+    def __init__(self, torch, n_in: int, n_out: int, width: int = 256, depth: int = 4, seed: int = 0,
+                 split_input: bool = True):
         self.torch = torch
         self.n_in, self.n_out, self.width, self.depth = n_in, n_out, width, depth
-        self.k_in = _pad(n_in, 32)
+        # split_input: each feature enters as a (high, low) BF16 pair sharing one weight, so the
+        # first layer sees ~16 significant bits of the input (BF16 alone resolves T to ~4 K).
+        self.split = split_input
+        self.k_half = _pad(n_in, 16) if split_input else _pad(n_in, 32)
+        self.k_in = _pad(2 * self.k_half, 32) if split_input else self.k_half
         self.n_out_pad = _pad(n_out, 32)
         dims = [self.k_in] + [width] * depth + [self.n_out_pad]
         self.dims = dims
@@ -54,7 +59,8 @@ class SurrogateMLP:
         self.W, self.b, self.Wb = [], [], []
         self.mW, self.vW, self.mb, self.vb = [], [], [], []
         for li in range(len(dims) - 1):
-            fan_in, fan_out = dims[li], dims[li + 1]
+            fan_in = self.k_half if li == 0 else dims[li]
+            fan_out = dims[li + 1]
             valid_in = n_in if li == 0 else fan_in
             valid_out = n_out if li == len(dims) - 2 else fan_out
             w = torch.zeros(fan_out, fan_in, dtype=torch.float32)
@@ -69,8 +75,28 @@ class SurrogateMLP:
                 lst.append(torch.zeros_like(w))
             for lst in (self.mb, self.vb):
                 lst.append(torch.zeros(fan_out, dtype=torch.float32, device="cuda"))
+        if self.split:
+            self.Wb[0] = torch.zeros(dims[1], self.k_in, dtype=torch.bfloat16, device="cuda")
+            self._refresh_first_layer()
         self.step_count = 0
         self.norm: Optional[Normalizer] = None
+
+    def _refresh_first_layer(self):
+        check(lib().pgb_mlp_dup_weight_bf16(_ptr(self.W[0]), self.dims[1], self.k_half, _ptr(self.Wb[0]),
+                                            self.k_in, None), "dup_weight")
+
+    def prepare_input(self, x):
+        """(B, n_in) FP32 normalised features -> (B, k_in) BF16 network input."""
+        torch = self.torch
+        x = x.float().contiguous()
+        B = x.shape[0]
+        X = torch.zeros(B, self.k_in, dtype=torch.bfloat16, device="cuda")
+        if self.split:
+            check(lib().pgb_mlp_split_rows_bf16(_ptr(x), B, self.n_in, x.stride(0), _ptr(X), self.k_in,
+                                                self.k_half, None), "split_rows")
+        else:
+            X[:, :self.n_in] = x.to(torch.bfloat16)
+        return X
 
     # ------------------------------------------------------------------ kernels
     def _gemm(self, A, B, M, N, K, bias=None, act=0, pre=None, out_bf16=None, out_f32=None, ldo=None,
@@ -118,10 +144,13 @@ class SurrogateMLP:
             N, K = self.dims[li + 1], self.dims[li]
             gb_l = torch.empty(N, dtype=torch.float32, device="cuda")
             check(lib().pgb_mlp_bias_grad(_ptr(d_f32), B, N, N, _ptr(gb_l), None), "bias_grad")
-            gW_l = torch.empty(N, K, dtype=torch.float32, device="cuda")
+            # layer 0 of a split input: dL/dW = dZ^T x, with x ~ its high half (the gradient does
+            # not need the extra bits)
+            Kw = self.k_half if (li == 0 and self.split) else K
+            gW_l = torch.empty(N, Kw, dtype=torch.float32, device="cuda")
             dT = self._t(d_bf, B, N)             # (N, B)
-            XT = self._t(acts[li], B, K)         # (K, B)
-            self._gemm(dT, XT, N, K, B, out_f32=gW_l)
+            XT = self._t(acts[li], B, Kw)        # (Kw, B)
+            self._gemm(dT, XT, N, Kw, B, out_f32=gW_l)
             gW[li], gb[li] = gW_l, gb_l
             if li == 0:
                 break
@@ -147,11 +176,14 @@ class SurrogateMLP:
     def adam(self, gW, gb, lr=1e-3, b1=0.9, b2=0.999, eps=1e-8):
         self.step_count += 1
         for li in range(len(self.W)):
+            wb = None if (li == 0 and self.split) else self.Wb[li]
             check(lib().pgb_mlp_adam(_ptr(self.W[li]), _ptr(gW[li]), _ptr(self.mW[li]), _ptr(self.vW[li]),
-                                     _ptr(self.Wb[li]), self.W[li].numel(), lr, b1, b2, eps, self.step_count,
+                                     _ptr(wb), self.W[li].numel(), lr, b1, b2, eps, self.step_count,
                                      None), "adam")
             check(lib().pgb_mlp_adam(_ptr(self.b[li]), _ptr(gb[li]), _ptr(self.mb[li]), _ptr(self.vb[li]),
                                      None, self.b[li].numel(), lr, b1, b2, eps, self.step_count, None), "adam")
+        if self.split:
+            self._refresh_first_layer()
 
     def train_step(self, X, T, lr=1e-3) -> float:
         Y = self.forward(X, keep=True)
@@ -162,7 +194,7 @@ class SurrogateMLP:
 
     def state_dict(self):
         return {"W": [w.cpu() for w in self.W], "b": [b.cpu() for b in self.b], "dims": self.dims,
-                "n_in": self.n_in, "n_out": self.n_out, "norm": self.norm}
+                "n_in": self.n_in, "n_out": self.n_out, "split": self.split, "norm": self.norm}
 
 
 # ---------------------------------------------------------------------- features and data
@@ -193,14 +225,14 @@ def fit_normalizer(x: np.ndarray, y: np.ndarray) -> Normalizer:
 
 def generate_bdf_data(torch, cfg, ncell: int, seed: int, options: str = "gb.precision=mixed",
                       chunk: int = 1 << 20):
-    """(state, forcing) -> (state after dt_react) pairs from this library's GPU BDF."""
+    """(state, forcing) -> (state after dt_react, RHS evaluations) from this library's GPU BDF."""
     from .reactor import BoxArrays, ReactorBase
     from .workloads import make_cells
     cs = make_cells(cfg, ncell, seed=seed)
     ns = cs.rY.shape[1]
     r = ReactorBase.create("ReactorCvode", cfg.mech, f"ode.rtol={cfg.rtol} ode.atol={cfg.atol} " + options)
     r.init(2, 1)
-    outs_rY, outs_T = [], []
+    outs_rY, outs_T, outs_FC = [], [], []
     for c0 in range(0, ncell, chunk):
         c1 = min(ncell, c0 + chunk)
         n = c1 - c0
@@ -216,5 +248,66 @@ def generate_bdf_data(torch, cfg, ncell: int, seed: int, options: str = "gb.prec
         torch.cuda.synchronize()
         outs_rY.append(box.rY.view(ns, n).T.contiguous())
         outs_T.append(box.T.view(n).clone())
+        outs_FC.append(box.FC.view(n).clone())
     r.close()
-    return cs, torch.cat(outs_rY), torch.cat(outs_T)
+    return cs, torch.cat(outs_rY), torch.cat(outs_T), torch.cat(outs_FC)
+
+
+# ---------------------------------------------------------------------- trained-file reader
+def read_pgbs(path: str) -> dict:
+    """Parses a surrogate file (layout in csrc/surrogate_io.cu) into numpy arrays."""
+    import struct
+    b = open(path, "rb").read()
+    if b[:8] != b"PGBSURR1":
+        raise ValueError(f"{path}: not a surrogate file")
+    mech = b[8:40].rstrip(b"\0").decode()
+    hdr = struct.unpack("<16i", b[40:104])
+    ns, nmodel, nlayer, n_in, k_half, k_in, n_out, n_out_pad, nel, split = hdr[:10]
+    off = [104]
+
+    def arr(dt, n):
+        a = np.frombuffer(b, dtype=dt, count=n, offset=off[0])
+        off[0] += a.nbytes
+        return a.copy()
+
+    d = dict(mech=mech, ns=ns, nmodel=nmodel, nlayer=nlayer, n_in=n_in, k_half=k_half, k_in=k_in, n_out=n_out,
+             n_out_pad=n_out_pad, nel=nel, split=bool(split))
+    d["dims"] = arr("<i4", nlayer + 1)
+    d["out_species"] = arr("<i4", n_out)
+    for k in ("x_mean", "x_std", "z_min", "z_max"):
+        d[k] = arr("<f8", n_in)
+    d["y_scale"] = arr("<f8", n_out)
+    d["A"] = arr("<f8", nel * ns).reshape(nel, ns)
+    d["P"] = arr("<f8", ns * nel).reshape(ns, nel)
+    g = arr("<f8", 16)
+    d["gates"] = dict(zip(("ood_margin", "mis", "cons", "disT", "disY", "neg", "tol_T", "tol_Y", "audit"), g[:9]))
+    d["W"], d["b"] = [], []
+    for _ in range(nmodel):
+        Ws, bs = [], []
+        for l in range(nlayer):
+            N = int(d["dims"][l + 1])
+            K = k_half if (l == 0 and split) else int(d["dims"][l])
+            Ws.append(arr("<f4", N * K).reshape(N, K))
+            bs.append(arr("<f4", N))
+        d["W"].append(Ws)
+        d["b"].append(bs)
+    if off[0] != len(b):
+        raise ValueError(f"{path}: {len(b) - off[0]} trailing bytes")
+    return d
+
+
+def models_from_pgbs(torch, d: dict) -> List["SurrogateMLP"]:
+    """SurrogateMLP objects carrying a trained file's weights (for checks of the fused kernel)."""
+    out = []
+    for mi in range(d["nmodel"]):
+        m = SurrogateMLP(torch, d["n_in"], d["n_out"], width=int(d["dims"][1]), depth=d["nlayer"] - 1,
+                         split_input=d["split"])
+        for l in range(d["nlayer"]):
+            m.W[l].copy_(torch.tensor(d["W"][mi][l]))
+            m.b[l].copy_(torch.tensor(d["b"][mi][l]))
+            if l > 0 or not m.split:
+                m.Wb[l].copy_(m.W[l].to(torch.bfloat16))
+        if m.split:
+            m._refresh_first_layer()
+        out.append(m)
+    return out

@@ -1,0 +1,353 @@
+"""Trains the learned chemistry surrogate and writes the file the reactor loads (gb.surrogate).
+
+    python -m pelelm_gb300.surrogate_train --config drm19_2M --samples 4194304 \\
+        --out pelelm_gb300/data/drm19_syn.pgbs
+
+Steps, all on the GPU:
+  1. teacher data: states and forcing drawn from the workload's distribution, advanced over
+     dt_react by this library's BDF reactor (the plain method, at the workload's rtol/atol);
+  2. targets: the chemical increment per unit initial mass, dY_chem = (rhoY_new - rhoY - dt F) /
+     rho, for every species that takes part in a reaction (inert species have none), and dT;
+     features x = [log10 max(Y, 1e-14), T, F / rho, F_h / rho], both standardised;
+  3. an ensemble of MLPs (4 x 256 GELU, BF16 weights, FP32 accumulation and master weights)
+     trained with Adam by this library's BF16 tensor-core kernels (pelelm_gb300.surrogate);
+  4. gate calibration on held-out cells: the fused kernel's checks (out-of-distribution,
+     enthalpy consistency, element conservation, ensemble disagreement, negativity) are emulated
+     in FP64 and the thresholds that keep the most BDF work off the fallback path are chosen
+     subject to the accepted cells' largest |T| and |Y| errors staying under a safety fraction
+     of the tolerances (default 1 K and 1e-4, safety 0.5);
+  5. the .pgbs file (layout in csrc/surrogate_io.cu).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import struct
+import sys
+import time
+from typing import Dict, List
+
+import numpy as np
+
+from .mech.model import R_ERG
+from .workloads import CONFIGS, load_mechanism
+
+
+# ---------------------------------------------------------------------- mechanism-derived tables
+def active_species(mech) -> List[int]:
+    """Species that appear as a reactant or product of some reaction."""
+    names = set()
+    for r in mech.reactions:
+        names.update(r.reactants.keys())
+        names.update(r.products.keys())
+    return sorted(mech.index(n) for n in names)
+
+
+def element_projection(mech, active: List[int]):
+    """A (nel x ns): atoms of element e per gram of species k, restricted to active species,
+    keeping a linearly independent set of element rows; P = A^T (A A^T)^-1 (ns x nel)."""
+    W = np.array([s.W for s in mech.species])
+    A = np.zeros((len(mech.elements), mech.ns))
+    for k in active:
+        for e, n in mech.species[k].composition.items():
+            A[mech.elements.index(e), k] = n / W[k]
+    rows: List[int] = []
+    for e in range(A.shape[0]):
+        if not A[e].any():
+            continue
+        trial = A[rows + [e]]
+        if np.linalg.matrix_rank(trial) == len(rows) + 1:
+            rows.append(e)
+    A = A[rows]
+    P = A.T @ np.linalg.inv(A @ A.T)
+    return A, P
+
+
+class Thermo:
+    """NASA-7 h_k(T), cp_k(T) per unit mass and T from (h, Y), on torch tensors (FP64)."""
+
+    def __init__(self, torch, mech):
+        dev = "cuda"
+        self.torch = torch
+        self.lo = torch.tensor([s.low for s in mech.species], device=dev, dtype=torch.float64)
+        self.hi = torch.tensor([s.high for s in mech.species], device=dev, dtype=torch.float64)
+        self.tm = torch.tensor([s.Tmid for s in mech.species], device=dev, dtype=torch.float64)
+        self.W = torch.tensor([s.W for s in mech.species], device=dev, dtype=torch.float64)
+
+    def h_cp(self, T):
+        T = T[:, None]
+        lo, hi = self.lo, self.hi
+
+        def hRT(a):
+            return (a[:, 0] + a[:, 1] * T / 2 + a[:, 2] * T ** 2 / 3 + a[:, 3] * T ** 3 / 4
+                    + a[:, 4] * T ** 4 / 5 + a[:, 5] / T)
+
+        def cpR(a):
+            return a[:, 0] + a[:, 1] * T + a[:, 2] * T ** 2 + a[:, 3] * T ** 3 + a[:, 4] * T ** 4
+
+        up = T >= self.tm
+        h = self.torch.where(up, hRT(hi), hRT(lo)) * R_ERG * T / self.W
+        cp = self.torch.where(up, cpR(hi), cpR(lo)) * R_ERG / self.W
+        return h, cp
+
+    def hy2t(self, hm, Y, T, iters: int = 20):
+        torch = self.torch
+        for _ in range(iters):
+            h, cp = self.h_cp(T)
+            dT = ((hm - (h * Y).sum(1)) / (cp * Y).sum(1)).clamp(-100.0, 100.0)
+            T = (T + dT).clamp(90.0, 5000.0)
+        return T
+
+
+# ---------------------------------------------------------------------- data
+def raw_features(torch, rY, T, F, Fh):
+    """Cell-major FP64 state -> FP32 features (the fused kernel computes the same in FP32)."""
+    rho = rY[:, :1].clone()
+    for k in range(1, rY.shape[1]):  # species in order, as the fused kernel sums them
+        rho = rho + rY[:, k:k + 1]
+    inv_rho = 1.0 / rho
+    Y = (rY * inv_rho).float()
+    return torch.cat([torch.log10(torch.clamp(Y, min=1e-14)), T[:, None].float(), (F * inv_rho).float(),
+                      (Fh[:, None] * inv_rho).float()], dim=1)
+
+
+def normalise(torch, x, x_mean, x_std):
+    """z = (x - mean) * (1 / std) in FP32 with FP32-rounded constants, as the fused kernel."""
+    m = torch.as_tensor(x_mean, device=x.device).float()
+    s = (1.0 / torch.as_tensor(x_std, device=x.device, dtype=torch.float64)).float()
+    return (x.float() - m) * s
+
+
+def make_dataset(torch, cfg, n: int, seed: int, options: str = "gb.precision=mixed") -> Dict[str, object]:
+    from .surrogate import generate_bdf_data
+    cs, rY1, T1, FC = generate_bdf_data(torch, cfg, n, seed=seed, options=options)
+    dev = "cuda"
+    d = {
+        "rY0": torch.tensor(cs.rY, device=dev), "T0": torch.tensor(cs.T, device=dev),
+        "F": torch.tensor(cs.rYsrc, device=dev), "Fh": torch.tensor(cs.rEsrc, device=dev),
+        "rE0": torch.tensor(cs.rE, device=dev), "rY1": rY1, "T1": T1, "FC": FC,
+    }
+    rho = d["rY0"].sum(1, keepdim=True)
+    d["rho0"] = rho
+    d["dYc"] = (rY1 - d["rY0"] - cfg.dt * d["F"]) / rho
+    d["dT"] = T1 - d["T0"]
+    d["x"] = raw_features(torch, d["rY0"], d["T0"], d["F"], d["Fh"])
+    return d
+
+
+def subset(d, sl):
+    return {k: v[sl] for k, v in d.items()}
+
+
+# ---------------------------------------------------------------------- training
+def train_models(torch, X, Tn, n_in, n_out, n_models: int, epochs: int, batch: int, lr: float, log=print,
+                 width: int = 256, depth: int = 4):
+    from .surrogate import SurrogateMLP
+    models = []
+    ntr = X.shape[0]
+    for mi in range(n_models):
+        m = SurrogateMLP(torch, n_in, n_out, width=width, depth=depth, seed=mi)
+        g = torch.Generator(device="cuda").manual_seed(1000 + mi)
+        Tp = torch.nn.functional.pad(Tn, (0, m.n_out_pad - n_out))
+        t0 = time.time()
+        for ep in range(epochs):
+            lr_ep = lr * 0.5 * (1.0 + math.cos(math.pi * ep / epochs)) + 1e-6
+            perm = torch.randperm(ntr, device="cuda", generator=g)
+            last = None
+            for i in range(0, ntr - batch + 1, batch):
+                idx = perm[i:i + batch]
+                last = m.train_step(X[idx], Tp[idx], lr=lr_ep)
+            if ep % 10 == 9 or ep == epochs - 1:
+                log(f"model {mi} epoch {ep + 1}/{epochs} batch loss {float(last) / (batch * n_out):.3e} "
+                    f"({time.time() - t0:.1f} s)")
+        models.append(m)
+    return models
+
+
+def predict(models, X, n_out):
+    return [m.forward(X)[:, :n_out].double() for m in models]
+
+
+# ---------------------------------------------------------------------- gates
+def apply_prediction(torch, thermo, st, preds, ys, out_species, A, P, dt):
+    """FP64 restatement of the fused kernel's update (surrogate_kernel.cuh, step 3) from the
+    members' normalised outputs: ensemble mean and spread, least-norm element-conservation
+    correction, new rhoY, rhoH and T from h(T) = rhoH / rho. st: rY0, F, rE0, Fh, T0 (cell-major)."""
+    ns = st["rY0"].shape[1]
+    n = st["rY0"].shape[0]
+    ys = torch.as_tensor(ys, device="cuda", dtype=torch.float64)
+    o = [p * ys for p in preds]
+    mean = sum(o) / len(o)
+    dis = (o[0] - o[1]).abs() if len(o) > 1 else torch.zeros_like(mean)
+    dY = torch.zeros(n, ns, device="cuda", dtype=torch.float64)
+    out_species = [int(s) for s in out_species]
+    sp = torch.tensor([s for s in out_species if s >= 0], device="cuda")
+    jt = out_species.index(-1)
+    js = [j for j, s in enumerate(out_species) if s >= 0]
+    dY[:, sp] = mean[:, js]
+    At = torch.as_tensor(A, device="cuda", dtype=torch.float64)
+    Pt = torch.as_tensor(P, device="cuda", dtype=torch.float64)
+    corr = -(dY @ At.T) @ Pt.T
+    dY = dY + corr
+    rho0 = st["rY0"].sum(1, keepdim=True)
+    rY1 = st["rY0"] + dt * st["F"] + rho0 * dY
+    rho1 = rY1.sum(1, keepdim=True)
+    Y1 = rY1 / rho1
+    rE1 = st["rE0"] + dt * st["Fh"]
+    Tp = st["T0"] + mean[:, jt]
+    Th = thermo.hy2t(rE1 / rho1[:, 0], Y1, Tp)
+    return dict(rY1=rY1, Y1=Y1, rE1=rE1, T=Th, Tp=Tp, cons=corr.abs().max(1).values, mis=(Th - Tp).abs(),
+                disT=dis[:, jt], disY=dis[:, js].max(1).values, neg=-Y1.min(1).values)
+
+
+def gate_quantities(torch, thermo, d, preds, ys, out_species, A, P, dt, zmin, zmax, z, margin):
+    """Per-cell check quantities of the fused kernel and the errors of its result against the
+    teacher (the BDF) on the cells of d."""
+    u = apply_prediction(torch, thermo, d, preds, ys, out_species, A, P, dt)
+    zt = torch.as_tensor
+    ood = ((z < zt(zmin - margin, device="cuda")) | (z > zt(zmax + margin, device="cuda"))).any(1)
+    Ytrue = d["rY1"] / d["rY1"].sum(1, keepdim=True)
+    return dict(cons=u["cons"], mis=u["mis"], disT=u["disT"], disY=u["disY"], neg=u["neg"], ood=ood,
+                eY=(u["Y1"] - Ytrue).abs().max(1).values, eT=(u["T"] - d["T1"]).abs())
+
+
+def calibrate(torch, q, FC, tol_T: float, tol_Y: float, safety: float, neg: float, log=print):
+    """Largest BDF work kept off the fallback path with max errors <= safety * tolerances.
+    Thresholds: enthalpy mismatch and ensemble |dT| spread <= aT; conservation correction and
+    ensemble |dY| spread <= aY; predicted mass fractions >= -neg."""
+    base = (~q["ood"]) & (q["neg"] <= neg)
+    fc = FC.double()
+    total = float(fc.sum())
+    best = None
+    for aT in np.geomspace(0.01, 20.0, 28):
+        okT = base & (q["mis"] <= aT) & (q["disT"] <= aT)
+        for aY in np.geomspace(1e-7, 3e-2, 28):
+            acc = okT & (q["cons"] <= aY) & (q["disY"] <= aY)
+            na = int(acc.sum())
+            if na == 0:
+                continue
+            if float(q["eT"][acc].max()) > safety * tol_T or float(q["eY"][acc].max()) > safety * tol_Y:
+                continue
+            saved = float(fc[acc].sum())
+            if best is None or saved > best[0]:
+                best = (saved, float(aT), float(aY), na)
+    if best is None:
+        log("calibration: no threshold pair meets the tolerances; the surrogate will reject every cell")
+        return dict(mis=0.0, disT=0.0, cons=0.0, disY=0.0, accept=0.0, work_saved=0.0)
+    saved, aT, aY, na = best
+    n = q["eT"].shape[0]
+    log(f"calibration: aT {aT:.3g} K, aY {aY:.3g}: accept {na / n:.4f} of cells, "
+        f"{saved / total:.4f} of BDF work (RHS evaluations)")
+    return dict(mis=aT, disT=aT, cons=aY, disY=aY, accept=na / n, work_saved=saved / total)
+
+
+# ---------------------------------------------------------------------- file
+def write_pgbs(path, mech_name, ns, models, x_mean, x_std, zmin, zmax, ys, out_species, A, P, gates):
+    m0 = models[0]
+    nlayer = len(m0.W)
+    hdr = [ns, len(models), nlayer, m0.n_in, m0.k_half, m0.k_in, len(out_species), m0.n_out_pad, A.shape[0],
+           1 if m0.split else 0] + [0] * 6
+    with open(path, "wb") as f:
+        f.write(b"PGBSURR1")
+        f.write(mech_name.encode().ljust(32, b"\0")[:32])
+        f.write(struct.pack("<16i", *hdr))
+        f.write(np.asarray(m0.dims, dtype="<i4").tobytes())
+        f.write(np.asarray(out_species, dtype="<i4").tobytes())
+        for a in (x_mean, x_std, zmin, zmax, ys):
+            f.write(np.asarray(a, dtype="<f8").tobytes())
+        f.write(np.ascontiguousarray(A, dtype="<f8").tobytes())
+        f.write(np.ascontiguousarray(P, dtype="<f8").tobytes())
+        g = np.zeros(16)
+        g[:9] = [gates["ood_margin"], gates["mis"], gates["cons"], gates["disT"], gates["disY"], gates["neg"],
+                 gates["tol_T"], gates["tol_Y"], gates["audit"]]
+        f.write(g.astype("<f8").tobytes())
+        for m in models:
+            for W, b in zip(m.W, m.b):
+                f.write(W.detach().float().cpu().numpy().astype("<f4").tobytes())
+                f.write(b.detach().float().cpu().numpy().astype("<f4").tobytes())
+
+
+# ---------------------------------------------------------------------- driver
+def run(torch, config: str, samples: int, val: int, epochs: int, n_models: int, out: str,
+        tol_T: float = 1.0, tol_Y: float = 1e-4, safety: float = 0.5, audit: float = 0.01,
+        ood_margin: float = 0.05, neg: float = 1e-6, batch: int = 8192, lr: float = 1e-3, seed: int = 11,
+        log=print) -> Dict[str, object]:
+    cfg = CONFIGS[config]
+    mech = load_mechanism(cfg.mech)
+    act = active_species(mech)
+    out_species = act + [-1]
+    A, P = element_projection(mech, act)
+    t0 = time.time()
+    d = make_dataset(torch, cfg, samples + val, seed=seed)
+    t_data = time.time() - t0
+    log(f"teacher data: {samples + val} cells in {t_data:.1f} s")
+    tr, va = subset(d, slice(0, samples)), subset(d, slice(samples, None))
+    tgt = torch.cat([d["dYc"][:, act], d["dT"][:, None]], 1)
+    x = d["x"].double()
+    x_mean = x[:samples].mean(0)
+    x_std = x[:samples].std(0)
+    # features constant over the training states (absent intermediates, fixed radical seeds)
+    # keep unit scale: their z stays ~0 and the OOD range catches any departure
+    x_std = torch.where(x_std > 1e-6 * (x_mean.abs() + 1.0), x_std, torch.ones_like(x_std))
+    ys = tgt[:samples].std(0).clamp_min(1e-30)
+    z = normalise(torch, d["x"], x_mean, x_std)
+    zmin = z[:samples].min(0).values.double().cpu().numpy()
+    zmax = z[:samples].max(0).values.double().cpu().numpy()
+    from .surrogate import SurrogateMLP
+    probe = SurrogateMLP(torch, x.shape[1], len(out_species), seed=0)
+    X = probe.prepare_input(z)
+    del probe
+    Tn = (tgt / ys).float()
+    t1 = time.time()
+    models = train_models(torch, X[:samples], Tn[:samples], x.shape[1], len(out_species), n_models, epochs,
+                          batch, lr, log=log)
+    torch.cuda.synchronize()
+    t_train = time.time() - t1
+    thermo = Thermo(torch, mech)
+    preds = predict(models, X[samples:], len(out_species))
+    q = gate_quantities(torch, thermo, va, preds, ys, out_species, A, P, cfg.dt, zmin, zmax,
+                        z[samples:].double(), ood_margin)
+    # operating points: the configured tolerances first (stored in the file), then looser
+    # ones (the sidecar <out>.levels.json; gb.sg.* options select them at run time)
+    levels = []
+    for lt, ly in [(tol_T, tol_Y)] + [(f * tol_T, g * tol_Y) for f, g in ((2, 3), (5, 10), (10, 30))]:
+        ng = max(neg, 0.1 * ly)
+        cal = calibrate(torch, q, va["FC"], lt, ly, safety, ng, log=log)
+        levels.append(dict(tol_T=lt, tol_Y=ly, ood_margin=ood_margin, mis=cal["mis"], cons=cal["cons"],
+                           disT=cal["disT"], disY=cal["disY"], neg=ng, audit=audit,
+                           val_accept=cal["accept"], val_work_saved=cal["work_saved"]))
+    gates = {k: levels[0][k] for k in ("ood_margin", "mis", "cons", "disT", "disY", "neg", "tol_T", "tol_Y",
+                                       "audit")}
+    write_pgbs(out, mech.name, mech.ns, models, x_mean.cpu().numpy(), x_std.cpu().numpy(), zmin, zmax,
+               ys.cpu().numpy(), out_species, A, P, gates)
+    with open(out + ".levels.json", "w") as f:
+        json.dump({"safety": safety, "levels": levels}, f, indent=1)
+    ep = lambda e: float(torch.quantile(e[:100000].float(), 0.5))  # noqa: E731
+    summary = dict(config=config, samples=samples, val=val, epochs=epochs, models=n_models,
+                   data_s=round(t_data, 1), train_s=round(t_train, 1), levels=levels,
+                   val_median_eT_all=ep(q["eT"]), val_median_eY_all=ep(q["eY"]))
+    log(json.dumps(summary))
+    return summary
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--config", default="drm19_2M")
+    ap.add_argument("--samples", type=int, default=4194304)
+    ap.add_argument("--val", type=int, default=262144)
+    ap.add_argument("--epochs", type=int, default=150)
+    ap.add_argument("--models", type=int, default=2)
+    ap.add_argument("--tol-T", type=float, default=1.0)
+    ap.add_argument("--tol-Y", type=float, default=1e-4)
+    ap.add_argument("--safety", type=float, default=0.5)
+    ap.add_argument("--audit", type=float, default=0.01)
+    ap.add_argument("--out", required=True)
+    a = ap.parse_args(argv)
+    import torch
+    run(torch, a.config, a.samples, a.val, a.epochs, a.models, a.out, tol_T=a.tol_T, tol_Y=a.tol_Y,
+        safety=a.safety, audit=a.audit)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -124,6 +124,12 @@ def _boxes_cfg2() -> List[int]:
     return [int(s) for s in rng.permutation(sides)]
 
 
+def _boxes_cfg3() -> List[int]:
+    sides = [32] * 96 + [16] * 256  # 2^22 cells
+    rng = np.random.default_rng(1003)
+    return [int(s) for s in rng.permutation(sides)]
+
+
 def _boxes_cfg4() -> List[int]:
     sides = [64] * 2 + [32] * 14 + [16] * 14 + [8] * 16  # 2^20 cells
     rng = np.random.default_rng(1004)
@@ -145,6 +151,11 @@ CONFIGS: Dict[str, Config] = {
         phi=(0.6, 1.4), dT=(1900.0, 1900.0),
         description="drm19-shaped CH4/air (21 sp, 84 rx), 2^21 cells in 16^3/32^3 boxes, "
                     "dt_react 1e-5 s, forcing as lidryer_amr120"),
+    "drm19_4M": Config(
+        "drm19_4M", "drm19_syn", _boxes_cfg3(), dt=1e-5, forcing=True, fuel="CH4",
+        phi=(0.6, 1.4), dT=(1900.0, 1900.0),
+        description="drm19-shaped CH4/air, the drm19_2M state distribution on 2^22 cells in "
+                    "16^3/32^3 boxes (surrogate inference workload)"),
     "gri_1M": Config(
         "gri_1M", "gri_syn", _boxes_cfg4(), dt=1e-5, forcing=True, fuel="CH4",
         phi=(0.5, 1.5), dT=(2100.0, 2100.0), p_atm=(1.0, 10.0),

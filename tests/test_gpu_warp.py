@@ -1,0 +1,147 @@
+"""GPU parity of the warp-per-cell BDF kernel (gb.mapping=warp; the only mapping compiled for
+the GRI-shaped mechanism, 53 species / 325 reactions) against the CPU oracle, through the C ABI.
+
+The warp kernel sums production rates, norms and the energy closure in a different order than
+the oracle (lanes, shuffles), so a cell can take a different step sequence; FP64 mode is held
+to the plain method's tolerances (T within 1e-6 relative, rhoY within atol + rtol |rhoY|) on
+at least 99% of the cells and, like mixed precision, judged on all cells by its error against a
+tight oracle (rtol 1e-11), which must be no worse than the FP64 oracle's own error at the same
+rtol/atol.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from helpers import boxes_from_cells, gather, tol_ratio
+from pelelm_gb300.reactor import ReactorBase
+from pelelm_gb300.workloads import CONFIGS, make_cells, mech_path
+
+OUT = os.environ.get("PGB_TEST_OUT", "gpurun_out")
+
+
+def _report(name, d):
+    try:
+        os.makedirs(OUT, exist_ok=True)
+        with open(os.path.join(OUT, "parity_report.jsonl"), "a") as f:
+            f.write(json.dumps({"test": name, **d}) + "\n")
+    except OSError:
+        pass
+
+
+def _run(torch, cfg, cs, sides, opts, **kw):
+    boxes = boxes_from_cells(torch, cs, sides, **kw)
+    r = ReactorBase.create("ReactorCvode", cfg.mech, f"ode.rtol={cfg.rtol} ode.atol={cfg.atol} {opts}")
+    r.init(2, 1)
+    r.react_boxes(boxes, cfg.dt, 0.0)
+    torch.cuda.synchronize()
+    st = r.stats()
+    r.close()
+    return gather(boxes, cs.rY.shape[1]), st
+
+
+CASES = [("lidryer_amr120", 2048, [8, 8, 8, 8], "gb.mapping=warp"),
+         ("drm19_2M", 1024, [8, 8], "gb.mapping=warp"),
+         ("gri_1M", 256, [(8, 8, 4)], "")]
+
+
+def _errs(tight, rY, T):
+    Yt = tight[0] / tight[0].sum(1, keepdims=True)
+    Y = rY / rY.sum(1, keepdims=True)
+    dT = np.abs(T - tight[1])
+    dY = np.abs(Y - Yt).max(1)
+    return dT.max(), np.percentile(dT, 99), dY.max(), np.percentile(dY, 99)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("cfgname,n,sides,opts", CASES)
+def test_warp_kernel_against_oracle(native_lib, oracle_mod, cuda, cfgname, n, sides, opts, precision):
+    cfg = CONFIGS[cfgname]
+    cs = make_cells(cfg, n, seed=21)
+    (rYg, Tg, rEg, FCg), st = _run(cuda, cfg, cs, sides, f"{opts} gb.precision={precision}")
+    om = oracle_mod.OracleMech(mech_path(cfg.mech))
+    rYo, To, rEo, FCo, nf = om.react(cs.rY, cs.rYsrc, cs.T, cs.rE, cs.rEsrc, cs.mask, cfg.dt, cfg.rtol, cfg.atol)
+    tight = om.react(cs.rY, cs.rYsrc, cs.T, cs.rE, cs.rEsrc, cs.mask, cfg.dt, 1e-11, 1e-16, max_steps=200000)
+    relT = np.abs(Tg - To) / To
+    ratio = tol_ratio(rYg, rYo, cfg.rtol, cfg.atol).max(1)
+    within = (relT <= 1e-6) & (ratio <= 1.0)
+    eg, eo = _errs(tight, rYg, Tg), _errs(tight, rYo, To)
+    _report(f"warp[{cfgname},{precision}]", {
+        "frac_within_plain_tol": float(within.mean()), "max_relT": float(relT.max()),
+        "max_ratio": float(ratio.max()), "frac_same_nfe": float(np.mean(FCg == FCo)),
+        "nfe_gpu": float(FCg.mean()), "nfe_orc": float(FCo.mean()), "nfail": int(st["nfail"]),
+        "err_vs_tight_gpu": [float(x) for x in eg], "err_vs_tight_oracle": [float(x) for x in eo]})
+    assert st["nfail"] == 0 and nf == 0 and np.all(FCg > 0)
+    np.testing.assert_allclose(rEg, rEo, rtol=1e-14, atol=1e-14 * np.abs(rEo).max())
+    if precision == "fp64":
+        assert within.mean() >= 0.99, within.mean()
+    Tmax = float(np.max(tight[1]))
+    bounds = ((2.0, 50 * cfg.rtol * Tmax), (1.25, 1e-3), (2.0, 50 * cfg.rtol), (1.25, 1e-8))
+    for a, b, (fac, slack) in zip(eg, eo, bounds):
+        assert a <= fac * b + slack, (eg, eo)
+
+
+@pytest.mark.gpu
+def test_warp_kernel_boxes_ghosts_mask_graph(native_lib, oracle_mod, cuda):
+    """Uneven boxes with offsets, ghost cells and a mask in one launch, also from a CUDA graph."""
+    torch = cuda
+    cfg = CONFIGS["lidryer_amr120"]
+    shapes = [(8, 8, 8), (16, 4, 8), (5, 7, 3), (12, 6, 4)]
+    n = sum(a * b * c for a, b, c in shapes)
+    cs = make_cells(cfg, n, seed=3)
+    rng = np.random.default_rng(5)
+    cs.mask[:] = np.where(rng.uniform(size=n) < 0.1, -1, 1)
+    los = [(0, 0, 0), (8, -4, 2), (-3, 5, 100), (40, 40, 40)]
+    om = oracle_mod.OracleMech(mech_path(cfg.mech))
+    rYo, To, rEo, FCo, nf = om.react(cs.rY, cs.rYsrc, cs.T, cs.rE, cs.rEsrc, cs.mask, cfg.dt, cfg.rtol, cfg.atol)
+    stream = torch.cuda.Stream()
+    boxes = boxes_from_cells(torch, cs, shapes, lo_list=los, ghost=2, with_mask=True)
+    r = ReactorBase.create("ReactorCvode", cfg.mech, f"ode.rtol={cfg.rtol} ode.atol={cfg.atol} gb.graph=1 "
+                           "gb.precision=fp64 gb.mapping=warp")
+    r.init(2, 1)
+    for rep in range(2):
+        if rep:
+            boxes = boxes_from_cells(torch, cs, shapes, lo_list=los, ghost=2, with_mask=True)
+        with torch.cuda.stream(stream):
+            r.react_boxes(boxes, cfg.dt, 0.0, stream=stream)
+        stream.synchronize()
+        rYg, Tg, rEg, FCg = gather(boxes, cs.rY.shape[1])
+        covered = cs.mask < 0
+        assert np.all(FCg[covered] == 0) and np.all(FCg[~covered] > 0)
+        np.testing.assert_array_equal(Tg[covered], cs.T[covered])
+        np.testing.assert_array_equal(rYg[covered], cs.rY[covered])
+        relT = (np.abs(Tg - To) / To)[~covered]
+        assert np.mean(relT <= 1e-6) >= 0.99
+    r.close()
+
+
+@pytest.mark.gpu
+def test_warp_kernel_is_deterministic_and_serves_the_surrogate_fallback(native_lib, cuda):
+    """Two runs give identical bits (no atomics in the arithmetic); the surrogate's fallback
+    cells through the warp kernel equal the plain warp-kernel run bit for bit."""
+    torch = cuda
+    cfg = CONFIGS["drm19_2M"]
+    cs = make_cells(cfg, 4096, seed=31)
+    base = "gb.mapping=warp gb.precision=mixed"
+    (a, _), (b, _) = (_run(torch, cfg, cs, [16], base) for _ in range(2))
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
+    surr = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "pelelm_gb300", "data",
+                        "drm19_syn.pgbs")
+    with open(surr + ".levels.json") as f:
+        lv = json.load(f)["levels"][-1]
+    sg = " ".join(f"gb.sg.{k}={lv[k]!r}" for k in ("mis", "cons", "disT", "disY", "neg", "tol_T", "tol_Y"))
+    (g, _) = _run(torch, cfg, cs, [16], f"{base} gb.surrogate={surr} {sg}")
+    fb = g[3] != 0.0
+    assert fb.any() and (~fb).any()
+    assert np.array_equal(g[0][fb], a[0][fb]) and np.array_equal(g[1][fb], a[1][fb])
+
+
+@pytest.mark.gpu
+def test_gri_thread_mapping_and_pointwise_rates_are_refused(native_lib, cuda):
+    with pytest.raises(RuntimeError, match="cell-per-thread"):
+        ReactorBase.create("ReactorCvode", "gri_syn", "gb.mapping=thread")
+    with pytest.raises(RuntimeError, match="surrogate"):
+        ReactorBase.create("ReactorCvode", "gri_syn", "gb.surrogate=x.pgbs")
