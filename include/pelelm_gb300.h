@@ -105,6 +105,21 @@ typedef struct pgb_surrogate_stats {
 } pgb_surrogate_stats;
 int pgb_reactor_get_surrogate_stats(pgb_reactor* r, pgb_surrogate_stats* out);
 
+/* Raw outputs of the reactor's surrogate ensemble for every cell of the boxes (flat cell order),
+ * FP32 [cell][member][n_out] in normalised units, through the fused inference kernel; the
+ * state is not modified and no gate is applied. in_rows (optional): the network input rows
+ * [cell][k_in] (split BF16 features, as FP32). Diagnostics and kernel-vs-training checks; no
+ * counterpart in the reference. out, in_rows: device memory. */
+int pgb_reactor_surrogate_raw(pgb_reactor* r, const pgb_box_view* views, int nbox, float* out,
+                              float* in_rows, void* stream);
+
+/* Surrogate input features of every cell of the boxes (flat cell order, boxes in order, i
+ * fastest), FP32, row-major [cell][2 NS + 2]: log10 max(Y_k, 1e-14), T, F_rhoY_k / rho,
+ * F_rhoh / rho; masked cells get zeros. The same device code the inference kernel uses, so
+ * training sets see the kernel's bits. out: device memory. No counterpart in the reference. */
+int pgb_surrogate_features(const char* mechanism, const pgb_box_view* views, int nbox, float* out,
+                           void* stream);
+
 /* ReactorBase::close (Source/PeleLM.cpp:930) and destruction. */
 void pgb_reactor_close(pgb_reactor* r);
 

@@ -52,6 +52,8 @@ EXPORTS = {
                                           C.c_double, _vp]),
     "pgb_reactor_get_stats": (C.c_int, [_vp, C.POINTER(Stats)]),
     "pgb_reactor_get_surrogate_stats": (C.c_int, [_vp, C.POINTER(SurrogateStats)]),
+    "pgb_surrogate_features": (C.c_int, [C.c_char_p, _vp, C.c_int, _vp, _vp]),
+    "pgb_reactor_surrogate_raw": (C.c_int, [_vp, _vp, C.c_int, _vp, _vp, _vp]),
     "pgb_reactor_close": (None, [_vp]),
     "pgb_reaction_rates": (C.c_int, [C.c_char_p, C.POINTER(BoxView), C.POINTER(Array4), _vp]),
     "pgb_rhoh_to_temp": (C.c_int, [C.c_char_p, C.POINTER(BoxView), C.c_double, C.c_double, _vp]),

@@ -19,7 +19,9 @@
 
 namespace pgb {
 
-__device__ __constant__ static const double kExp64Table[64] = PGB_EXP64_TABLE;
+// Tables in global memory, read through L1: lanes look up different entries, which the
+// constant cache would serialize.
+__device__ static const double kExp64Table[64] = PGB_EXP64_TABLE;
 
 __device__ __forceinline__ double pgb_exp64(double x) {
   constexpr double kShift = 6755399441055744.0;  // 1.5 * 2^52
@@ -33,7 +35,7 @@ __device__ __forceinline__ double pgb_exp64(double x) {
   p = fma(r2, p, r);
   const int j = n & 63;
   const int m = n >> 6;
-  const double s = kExp64Table[j];
+  const double s = __ldg(&kExp64Table[j]);
   const double v = fma(s, p, s);
   const int hi = __double2hiint(v) + (m << 20);
   double res = __hiloint2double(hi, __double2loint(v));
@@ -48,8 +50,8 @@ __device__ __forceinline__ double pgb_exp64(double x) {
 // Eleven FP64 pipe instructions (r through one FMA with a tabulated 1/c_j; the exponent and
 // table index come from integer ops). Defined for positive normal x, the only arguments the
 // rate code passes (temperatures, clipped reduced pressures, Troe centring factors).
-__device__ __constant__ static const double kLog64InvC[64] = PGB_LOG64_INVC;
-__device__ __constant__ static const double kLog64LogC[64] = PGB_LOG64_LOGC;
+__device__ static const double kLog64InvC[64] = PGB_LOG64_INVC;
+__device__ static const double kLog64LogC[64] = PGB_LOG64_LOGC;
 
 __device__ __forceinline__ double pgb_log64(double x) {
   const int hi = __double2hiint(x);
@@ -57,12 +59,12 @@ __device__ __forceinline__ double pgb_log64(double x) {
   const int e = ((hi >> 20) & 0x7ff) - 1023;
   const int j = (hi >> 14) & 63;
   const double m = __hiloint2double((hi & 0x000fffff) | 0x3ff00000, lo);
-  const double r = fma(m, kLog64InvC[j], -1.0);
+  const double r = fma(m, __ldg(&kLog64InvC[j]), -1.0);
   const double r2 = r * r;
   double p = fma(r, fma(r, fma(r, fma(r, fma(r, 1.0 / 7.0, -1.0 / 6.0), 0.2), -0.25), 1.0 / 3.0), -0.5);
   p = fma(r2, p, r);
   const double ed = (double)e;
-  return fma(ed, PGB_LOG64_LN2_HI, kLog64LogC[j] + fma(ed, PGB_LOG64_LN2_LO, p));
+  return fma(ed, PGB_LOG64_LN2_HI, __ldg(&kLog64LogC[j]) + fma(ed, PGB_LOG64_LN2_LO, p));
 }
 
 // x^a for x > 0 through the two functions above (step-size heuristics).

@@ -5,6 +5,8 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "../../include/pelelm_gb300.h"
 #include "bdf_kernel.cuh"
 #include "bdf_warp_kernel.cuh"
@@ -122,6 +124,14 @@ int launch_surrogate_audit(const pgb::SurrogateParams& p, cudaStream_t s, int nb
   return 0;
 }
 
+template <class M>
+int launch_surrogate_features(const pgb::BoxDev* boxes, int nbox, long long ncell, float* out, cudaStream_t s) {
+  const long long nb = std::min<long long>((ncell + 255) / 256, 4096);
+  pgb::surrogate_features_kernel<M><<<(int)std::max<long long>(nb, 1), 256, 0, s>>>(boxes, nbox, ncell, out);
+  PGB_CUDA(cudaGetLastError());
+  return 0;
+}
+
 struct MechEntry {
   const char* name;
   int ns, nr;
@@ -136,6 +146,7 @@ struct MechEntry {
   int (*sg_audit_fn)(const pgb::SurrogateParams&, cudaStream_t, int);
   LaunchFn warp_mixed, warp_fp64;  // warp-per-cell BDF (argument: warps per block)
   int wsmem_mixed, wsmem_fp64;     // shared bytes per warp
+  int (*sg_feat_fn)(const pgb::BoxDev*, int, long long, float*, cudaStream_t);
 };
 
 
@@ -213,7 +224,7 @@ int h2t_entry(const pgb_box_view* v, double tmin, double tmax, cudaStream_t s) {
         ::pgb_host::h2t_entry<M>, ::pgb_host::launch_surrogate<M>,                           \
         ::pgb_host::launch_surrogate_audit<M>, ::pgb_host::launch_bdf_warp<M, float>,        \
         ::pgb_host::launch_bdf_warp<M, double>, pgb::bdf_warp_smem_per_warp<M, float>(),     \
-        pgb::bdf_warp_smem_per_warp<M, double>()                                             \
+        pgb::bdf_warp_smem_per_warp<M, double>(), ::pgb_host::launch_surrogate_features<M>   \
   }
 
 // Mechanisms too large for one cell per thread: warp-per-cell BDF, ReactorNull and T(h, Y) only.
@@ -222,7 +233,8 @@ int h2t_entry(const pgb_box_view* v, double tmin, double tmax, cudaStream_t s) {
     M::NAME, M::NS, M::NR, nullptr, nullptr, ::pgb_host::launch_null<M>, 0, 0, 0, 0, 0, 0,    \
         nullptr, ::pgb_host::h2t_entry<M>, nullptr, nullptr,                                 \
         ::pgb_host::launch_bdf_warp<M, float>, ::pgb_host::launch_bdf_warp<M, double>,       \
-        pgb::bdf_warp_smem_per_warp<M, float>(), pgb::bdf_warp_smem_per_warp<M, double>()    \
+        pgb::bdf_warp_smem_per_warp<M, float>(), pgb::bdf_warp_smem_per_warp<M, double>(),   \
+        nullptr                                                                              \
   }
 
 // Converts and validates one box view into its device descriptor; cell numbering of the box

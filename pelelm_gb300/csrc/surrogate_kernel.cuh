@@ -84,6 +84,9 @@ struct SurrogateParams {
   unsigned long long* audit_count;
   SurrogateStats* stats;
   unsigned long long* seed_dev;          // audit sample seed; advanced by the audit kernel
+  float* raw_out;                        // non-null: write the members' raw outputs
+                                         // [cell][member][n_out] and leave the state untouched
+  float* raw_in;                         // with raw_out: also the network input rows [cell][k_in]
 };
 
 __device__ __forceinline__ const BoxDev& sg_locate(const BoxDev* boxes, int nbox, long long c, int& i, int& j,
@@ -112,6 +115,24 @@ __device__ __forceinline__ double sg_uniform(unsigned long long x) {  // splitmi
   x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
   x ^= x >> 31;
   return (double)(x >> 11) * (1.0 / 9007199254740992.0);
+}
+
+// Raw features of one cell, in FP32, handed to put(q, x): log10 max(Y_k, 1e-14) (q < NS), T,
+// F_k / rho (q = NS+1 ..), F_h / rho. The one definition used by the inference kernel and by the
+// feature extraction that builds training sets (pgb_surrogate_features), so both see the same bits.
+template <class M, class F>
+__device__ __forceinline__ void sg_features(const BoxDev& B, int i, int j, int k, F&& put) {
+  constexpr int NS = M::NS;
+  double rho = 0.0;
+#pragma unroll
+  for (int s = 0; s < NS; ++s) rho += arr_at(B.rY, i, j, k, s);
+  const double inv_rho = 1.0 / rho;
+#pragma unroll
+  for (int s = 0; s < NS; ++s) put(s, log10f(fmaxf((float)(arr_at(B.rY, i, j, k, s) * inv_rho), 1e-14f)));
+  put(NS, (float)arr_at(B.T, i, j, k, 0));
+#pragma unroll
+  for (int s = 0; s < NS; ++s) put(NS + 1 + s, (float)(arr_at(B.rYsrc, i, j, k, s) * inv_rho));
+  put(2 * NS + 1, (float)(arr_at(B.rEsrc, i, j, k, 0) * inv_rho));
 }
 
 // One dense layer on the 128-row tile: out = act(in (128 x K) . W^T (K -> N) + b), N = NT * 16.
@@ -222,28 +243,24 @@ __global__ void __launch_bounds__(256, 1) surrogate_kernel(const SurrogateParams
         bf16* row = A0[tid];
         for (int q = 0; q < net.k_in; ++q) row[q] = __float2bfloat16(0.f);
         if (!masked) {
-          double rho = 0.0;
-#pragma unroll
-          for (int s = 0; s < NS; ++s) rho += arr_at(B->rY, i, j, k, s);
-          const double inv_rho = 1.0 / rho;
-          auto put = [&](int q, float x) {
-            const float z = (x - net.x_mean[q]) * net.x_inv_std[q];
+          sg_features<M>(*B, i, j, k, [&](int q, float x) {
+            // explicit roundings: a contraction into the last multiply of an inlined log10f
+            // would give other bits than the features training saw (pgb_surrogate_features)
+            const float z = __fmul_rn(__fsub_rn(x, net.x_mean[q]), net.x_inv_std[q]);
             if (!(z >= net.z_lo[q] && z <= net.z_hi[q])) ood = 1;
             const bf16 hi = __float2bfloat16(z);
             row[q] = hi;
             row[net.k_half + q] = __float2bfloat16(z - __bfloat162float(hi));
-          };
-#pragma unroll
-          for (int s = 0; s < NS; ++s)
-            put(s, log10f(fmaxf((float)(arr_at(B->rY, i, j, k, s) * inv_rho), 1e-14f)));
-          put(NS, (float)arr_at(B->T, i, j, k, 0));
-#pragma unroll
-          for (int s = 0; s < NS; ++s) put(NS + 1 + s, (float)(arr_at(B->rYsrc, i, j, k, s) * inv_rho));
-          put(2 * NS + 1, (float)(arr_at(B->rEsrc, i, j, k, 0) * inv_rho));
+          });
         }
         ood_flag[tid] = ood;
       }
       __syncthreads();
+      if (P.raw_in && mdl == 0)
+        for (int e = tid; e < SG_TILE * net.k_in; e += blockDim.x) {
+          const int rr = e / net.k_in, q = e - rr * net.k_in;
+          if (tile * SG_TILE + rr < P.ncell) P.raw_in[(size_t)(tile * SG_TILE + rr) * net.k_in + q] = __bfloat162float(A0[rr][q]);
+        }
       // ---- 2. layer stack
       bf16(*in)[SG_LDA] = A0;
       bf16(*out)[SG_LDA] = A1;
@@ -257,6 +274,14 @@ __global__ void __launch_bounds__(256, 1) surrogate_kernel(const SurrogateParams
       sg_layer<SG_NOUT_PAD / 16>(in, net.dims[L], net.W[mdl][L], net.b[mdl][L], Wsm, nullptr, O[mdl], net.n_out);
     }
 
+    if (P.raw_out) {  // raw network outputs only (diagnostics, kernel-vs-training checks)
+      if (tid < SG_TILE && c < P.ncell)
+        for (int mdl = 0; mdl < net.nmodel; ++mdl)
+          for (int q = 0; q < net.n_out; ++q)
+            P.raw_out[((size_t)c * net.nmodel + mdl) * net.n_out + q] = O[mdl][tid][q];
+      __syncthreads();
+      continue;
+    }
     // ---- 3. gates and update (warps 0..3: whole warps, so the ballots below are full)
     if (tid < SG_TILE) {
       SurrogateStats* S = P.stats;
@@ -373,6 +398,23 @@ __global__ void __launch_bounds__(256, 1) surrogate_kernel(const SurrogateParams
       }
     }
     __syncthreads();
+  }
+}
+
+// Raw features of every cell (flat cell order) into out[c * (2 NS + 2) + q]; masked cells get 0.
+template <class M>
+__global__ void surrogate_features_kernel(const BoxDev* boxes, int nbox, long long ncell, float* out) {
+  constexpr int NIN = 2 * M::NS + 2;
+  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < ncell; c += (long long)gridDim.x * blockDim.x) {
+    int i, j, k;
+    bool masked;
+    const BoxDev& B = sg_locate(boxes, nbox, c, i, j, k, masked);
+    float* o = out + c * NIN;
+    if (masked) {
+      for (int q = 0; q < NIN; ++q) o[q] = 0.f;
+    } else {
+      sg_features<M>(B, i, j, k, [&](int q, float x) { __stcg(o + q, x); });
+    }
   }
 }
 

@@ -499,6 +499,11 @@ def gen_tables(m: Mechanism, space: str = "constant") -> str:
         dnu = sum(r.products.values()) - sum(r.reactants.values())
         rx.append((math.log(r.rate.A), r.rate.beta, -r.rate.Ea / R_CAL, kind, int(r.reversible),
                    rs, ps, dnu, tb, tr))
+    if glob:
+        # warp-per-cell kernels give consecutive reactions to the lanes of a warp: group them by
+        # kind (elementary, third-body, falloff) so a 32-reaction pass rarely mixes code paths
+        order = sorted(range(len(rx)), key=lambda j: (rx[j][3], j))
+        rx = [rx[j] for j in order]
     maxeff = max([len(t) for t in tb_rows] + [1])
     e = _Emitter()
     e(f"// GENERATED by pelelm_gb300/mech/codegen.py (tables, {space} memory) from pelelm_gb300/data/{m.name}.json.")

@@ -128,6 +128,14 @@ class ReactorGB:
         check(lib().pgb_reactor_get_surrogate_stats(self._h, C.byref(s)), "get_surrogate_stats")
         return {n: getattr(s, n) for n, _ in _lib.SurrogateStats._fields_}
 
+    def surrogate_raw(self, boxes: List[BoxArrays], out, in_rows=None) -> None:
+        """Raw ensemble outputs [cell][member][n_out] (FP32 device tensor `out`) of the fused
+        inference kernel, optionally its input rows [cell][k_in]; the boxes are not modified."""
+        arr = (BoxView * len(boxes))(*[b.view() for b in boxes])
+        check(lib().pgb_reactor_surrogate_raw(self._h, arr, len(boxes), out.data_ptr(),
+                                              None if in_rows is None else in_rows.data_ptr(), None),
+              "surrogate_raw")
+
     def close(self) -> None:
         if self._h:
             lib().pgb_reactor_close(self._h)

@@ -223,16 +223,29 @@ def fit_normalizer(x: np.ndarray, y: np.ndarray) -> Normalizer:
     return Normalizer(x_mean=xm, x_std=xs, y_std=ys, x_min=z.min(0), x_max=z.max(0))
 
 
+def surrogate_features(torch, mechanism: str, boxes) -> "torch.Tensor":
+    """Raw FP32 surrogate features [cell][2 NS + 2] of the boxes' current state, computed by the
+    fused inference kernel's own device code (pgb_surrogate_features)."""
+    from ._lib import BoxView
+    n = sum(int(b.T.numel()) for b in boxes)
+    ns = int(boxes[0].rY.shape[0])
+    out = torch.empty(n, 2 * ns + 2, dtype=torch.float32, device="cuda")
+    arr = (BoxView * len(boxes))(*[b.view() for b in boxes])
+    check(lib().pgb_surrogate_features(mechanism.encode(), arr, len(boxes), _ptr(out), None), "surrogate_features")
+    return out
+
+
 def generate_bdf_data(torch, cfg, ncell: int, seed: int, options: str = "gb.precision=mixed",
                       chunk: int = 1 << 20):
-    """(state, forcing) -> (state after dt_react, RHS evaluations) from this library's GPU BDF."""
+    """(state, forcing) -> (state after dt_react, RHS evaluations, features of the initial
+    state) from this library's GPU BDF."""
     from .reactor import BoxArrays, ReactorBase
     from .workloads import make_cells
     cs = make_cells(cfg, ncell, seed=seed)
     ns = cs.rY.shape[1]
     r = ReactorBase.create("ReactorCvode", cfg.mech, f"ode.rtol={cfg.rtol} ode.atol={cfg.atol} " + options)
     r.init(2, 1)
-    outs_rY, outs_T, outs_FC = [], [], []
+    outs_rY, outs_T, outs_FC, outs_x = [], [], [], []
     for c0 in range(0, ncell, chunk):
         c1 = min(ncell, c0 + chunk)
         n = c1 - c0
@@ -244,13 +257,14 @@ def generate_bdf_data(torch, cfg, ncell: int, seed: int, options: str = "gb.prec
         box = BoxArrays(((0, 0, 0), (n - 1, 0, 0)), rY, dev(cs.rYsrc, ns).view(ns, 1, 1, n),
                         dev(cs.T, 1).view(1, 1, 1, n), dev(cs.rE, 1).view(1, 1, 1, n),
                         dev(cs.rEsrc, 1).view(1, 1, 1, n), torch.zeros(1, 1, 1, n, dtype=torch.float64, device="cuda"))
+        outs_x.append(surrogate_features(torch, cfg.mech, [box]))
         r.react_boxes([box], cfg.dt, 0.0)
         torch.cuda.synchronize()
         outs_rY.append(box.rY.view(ns, n).T.contiguous())
         outs_T.append(box.T.view(n).clone())
         outs_FC.append(box.FC.view(n).clone())
     r.close()
-    return cs, torch.cat(outs_rY), torch.cat(outs_T), torch.cat(outs_FC)
+    return cs, torch.cat(outs_rY), torch.cat(outs_T), torch.cat(outs_FC), torch.cat(outs_x)
 
 
 # ---------------------------------------------------------------------- trained-file reader

@@ -102,7 +102,9 @@ class Thermo:
 
 # ---------------------------------------------------------------------- data
 def raw_features(torch, rY, T, F, Fh):
-    """Cell-major FP64 state -> FP32 features (the fused kernel computes the same in FP32)."""
+    """Cell-major FP64 state -> FP32 features in torch: the definition of
+    surrogate_kernel.cuh's sg_features restated (tests compare the two; training and inference
+    use the kernel's own, pgb_surrogate_features)."""
     rho = rY[:, :1].clone()
     for k in range(1, rY.shape[1]):  # species in order, as the fused kernel sums them
         rho = rho + rY[:, k:k + 1]
@@ -121,7 +123,7 @@ def normalise(torch, x, x_mean, x_std):
 
 def make_dataset(torch, cfg, n: int, seed: int, options: str = "gb.precision=mixed") -> Dict[str, object]:
     from .surrogate import generate_bdf_data
-    cs, rY1, T1, FC = generate_bdf_data(torch, cfg, n, seed=seed, options=options)
+    cs, rY1, T1, FC, x = generate_bdf_data(torch, cfg, n, seed=seed, options=options)
     dev = "cuda"
     d = {
         "rY0": torch.tensor(cs.rY, device=dev), "T0": torch.tensor(cs.T, device=dev),
@@ -132,7 +134,7 @@ def make_dataset(torch, cfg, n: int, seed: int, options: str = "gb.precision=mix
     d["rho0"] = rho
     d["dYc"] = (rY1 - d["rY0"] - cfg.dt * d["F"]) / rho
     d["dT"] = T1 - d["T0"]
-    d["x"] = raw_features(torch, d["rY0"], d["T0"], d["F"], d["Fh"])
+    d["x"] = x  # the inference kernel's own featurisation of the initial states
     return d
 
 

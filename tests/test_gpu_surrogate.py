@@ -200,21 +200,37 @@ def test_fused_kernel_matches_unfused_network_and_fp64_update(drm19, cuda):
     models = models_from_pgbs(torch, d)
     dev = lambda a: torch.tensor(np.asarray(a), device="cuda")  # noqa: E731
     st = dict(rY0=dev(cs.rY), F=dev(cs.rYsrc), rE0=dev(cs.rE), Fh=dev(cs.rEsrc), T0=dev(cs.T))
-    x = raw_features(torch, st["rY0"], st["T0"], st["F"], st["Fh"])
+    from pelelm_gb300.surrogate import surrogate_features
+    x = surrogate_features(torch, cfg.mech, boxes_from_cells(torch, cs, drm19["sides"]))
+    xt = raw_features(torch, st["rY0"], st["T0"], st["F"], st["Fh"])
+    # the torch restatement of the featurisation agrees to a few FP32 ulps (log10 differs)
+    assert torch.allclose(x, xt, rtol=1e-6, atol=1e-6)
     X = models[0].prepare_input(normalise(torch, x, d["x_mean"], d["x_std"]))
-    preds = [m.forward(X)[:, :d["n_out"]].double() for m in models]
+    # raw network: the fused kernel's input rows and both members' outputs equal the training
+    # kernels' bit for bit
+    from pelelm_gb300.reactor import ReactorBase
+    rr = ReactorBase.create("ReactorCvode", cfg.mech, f"gb.surrogate={SURR}")
+    rr.init(2, 1)
+    raw = torch.empty(n, d["nmodel"], d["n_out"], device="cuda")
+    rin = torch.empty(n, d["k_in"], device="cuda")
+    rr.surrogate_raw(boxes_from_cells(torch, cs, drm19["sides"]), raw, rin)
+    torch.cuda.synchronize()
+    rr.close()
+    assert torch.equal(rin, X.float())
+    preds = [m.forward(X)[:, :d["n_out"]] for m in models]
+    for mi, p in enumerate(preds):
+        assert torch.equal(raw[:, mi, :], p), mi
+    preds = [p.double() for p in preds]
     u = apply_prediction(torch, Thermo(torch, load_mechanism(cfg.mech)), st, preds, d["y_scale"],
                          d["out_species"], d["A"], d["P"], cfg.dt)
     dT = np.abs(u["T"].cpu().numpy() - g[1])
     dY = np.abs(u["Y1"].cpu().numpy() - _Y(g[0])).max(1)
     _report("fused_vs_unfused", {"p999_dT": float(np.percentile(dT, 99.9)), "max_dT": float(dT.max()),
                                  "p999_dY": float(np.percentile(dY, 99.9)), "max_dY": float(dY.max())})
-    # the same arithmetic: almost every cell agrees to FP64 round-off. A one-ulp difference
-    # anywhere upstream (a transcendental, a reciprocal) can flip the BF16 rounding of a hidden
-    # activation, which moves that cell's output by up to ~1 K: the noise floor of BF16
-    # activations, bounded here
-    assert (dT <= 1e-6).mean() >= 0.95 and (dY <= 1e-10).mean() >= 0.95
-    assert dT.max() <= 3.0 and dY.max() <= 1e-3
+    # the same features, the same BF16 products in the same order: the network outputs agree
+    # bit for bit and the FP64 update to round-off (HY2T iterates, ensemble-mean order)
+    assert (dT <= 1e-6).mean() >= 0.999 and (dY <= 1e-10).mean() >= 0.999
+    assert dT.max() <= 1e-3 and dY.max() <= 1e-6
 
 
 @pytest.mark.gpu
@@ -276,16 +292,17 @@ def test_graph_replay_draws_a_new_audit_sample(drm19, cuda):
 @pytest.mark.gpu
 def test_bad_surrogate_files_are_rejected(native_lib, cuda, tmp_path):
     from pelelm_gb300.reactor import ReactorBase
+    # ReactorBase::create only names the reactor; init() builds it (as in the reference)
     with pytest.raises(RuntimeError, match="another mechanism"):
-        ReactorBase.create("ReactorCvode", "lidryer_syn", f"gb.surrogate={SURR}")
+        ReactorBase.create("ReactorCvode", "lidryer_syn", f"gb.surrogate={SURR}").init(2, 1)
     bad = tmp_path / "trunc.pgbs"
     bad.write_bytes(open(SURR, "rb").read()[:5000])
     with pytest.raises(RuntimeError, match="truncated"):
-        ReactorBase.create("ReactorCvode", "drm19_syn", f"gb.surrogate={bad}")
+        ReactorBase.create("ReactorCvode", "drm19_syn", f"gb.surrogate={bad}").init(2, 1)
     with pytest.raises(RuntimeError, match="cannot open"):
-        ReactorBase.create("ReactorCvode", "drm19_syn", f"gb.surrogate={tmp_path / 'missing.pgbs'}")
+        ReactorBase.create("ReactorCvode", "drm19_syn", f"gb.surrogate={tmp_path / 'missing.pgbs'}").init(2, 1)
     with pytest.raises(RuntimeError, match="ReactorCvode"):
-        ReactorBase.create("ReactorNull", "drm19_syn", f"gb.surrogate={SURR}")
+        ReactorBase.create("ReactorNull", "drm19_syn", f"gb.surrogate={SURR}").init(2, 1)
 
 
 @pytest.mark.gpu

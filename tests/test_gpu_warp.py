@@ -142,6 +142,6 @@ def test_warp_kernel_is_deterministic_and_serves_the_surrogate_fallback(native_l
 @pytest.mark.gpu
 def test_gri_thread_mapping_and_pointwise_rates_are_refused(native_lib, cuda):
     with pytest.raises(RuntimeError, match="cell-per-thread"):
-        ReactorBase.create("ReactorCvode", "gri_syn", "gb.mapping=thread")
+        ReactorBase.create("ReactorCvode", "gri_syn", "gb.mapping=thread").init(2, 1)
     with pytest.raises(RuntimeError, match="surrogate"):
-        ReactorBase.create("ReactorCvode", "gri_syn", "gb.surrogate=x.pgbs")
+        ReactorBase.create("ReactorCvode", "gri_syn", "gb.surrogate=x.pgbs").init(2, 1)
