@@ -59,6 +59,123 @@ __device__ __forceinline__ double warp_max(double v) {
   return v;
 }
 
+// The lane-distributed part of a length-N vector (element i in lane i % 32, slot i / 32).
+template <class M>
+struct WVec {
+  double v[(M::N + 31) / 32];
+};
+
+// Right-hand side f = [W_k wdot_k + F_k, dT/dt] at y, one warp cooperating (see the kernel
+// below). One non-inlined copy serves every call site: the step loop calls it from five places
+// and inlined copies of this exp/log-heavy body overflow the instruction cache.
+template <class M>
+__device__ __noinline__ WVec<M> warp_rhs(const WVec<M> yv, double* CS, double* GS, double* QS,
+                                         const double* FRC) {
+  using Tab = typename M::TabG;
+  constexpr int N = M::N, NS = M::NS, NR = M::NR;
+  constexpr int R = (N + 31) / 32;
+  const int lane = threadIdx.x & 31;
+  auto idx = [&](int r) { return lane + 32 * r; };
+  const double (&y)[R] = yv.v;
+  WVec<M> fv;
+  double (&f)[R] = fv.v;
+  auto bcast = [&](const double (&v)[R], int i) -> double {
+    return __shfl_sync(0xffffffffu, v[i >> 5], i & 31);
+  };
+  const double T = bcast(y, NS);
+  const double invT = 1.0 / T;
+  const double lnT = pgb_log64(T);
+  const double lnT1 = 1.0 - lnT;
+  const double lnP0RT = kLnP0OverR - lnT;
+  double c_loc = 0.0;
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const int k = idx(r);
+    if (k < NS) {
+      const TabSpecies<double>& s = Tab::template sp<double>(k);
+      const double c = y[r] * s.invW;
+      CS[k] = c;
+      c_loc += c;
+      const double* g = T < s.Tmid ? s.glo : s.ghi;
+      GS[k] = fma(g[0], lnT1, fma(T, fma(T, fma(T, fma(T, g[4], g[3]), g[2]), g[1]), fma(g[5], invT, g[6])));
+    }
+  }
+  const double Ctot = warp_sum(c_loc);
+  __syncwarp();
+  for (int j = lane; j < NR; j += 32) {
+    const TabReaction<double>& rx = Tab::template rx<double>(j);
+    const double lnkf = fma(rx.beta, lnT, fma(rx.mEaR, invT, rx.lnA));
+    double kf = pgb_exp64(lnkf);
+    double Mc = 1.0;
+    if (rx.tb >= 0) {
+      const TabThirdBody<double>& tb = Tab::template tb<double>(rx.tb);
+      Mc = Ctot;
+      for (int e = 0; e < tb.n; ++e) Mc = fma(tb.effm1[e], CS[tb.sp[e]], Mc);
+    }
+    if (rx.kind == 2) {
+      const TabTroe<double>& fo = Tab::template troe<double>(rx.troe);
+      const double lnk0 = fma(fo.beta0, lnT, fma(fo.mEa0R, invT, fo.lnA0));
+      const double Pr = Mc * pgb_exp64(lnk0 - lnkf);
+      double blend = Pr / (1.0 + Pr);
+      if (fo.ntroe > 0) {
+        double Fcent = fma(fo.one_m_a, pgb_exp64(T * fo.m_invT3), fo.a * pgb_exp64(T * fo.m_invT1));
+        if (fo.ntroe > 3) Fcent += pgb_exp64(invT * fo.m_T2);
+        const double lFc = pgb_log64(Fcent) * 0.4342944819032518;
+        const double cc = fma(-0.67, lFc, -0.4), nn = fma(-1.27, lFc, 0.75);
+        const double lPr = pgb_log64(fmax(Pr, 1e-300)) * 0.4342944819032518 + cc;
+        const double f1 = lPr / fma(-0.14, lPr, nn);
+        blend *= pgb_exp64(2.302585092994046 * lFc / fma(f1, f1, 1.0));
+      }
+      kf *= blend;
+    }
+    double Pf = 1.0, Pp = 1.0;
+    for (int s = 0; s < rx.nr; ++s) Pf *= CS[rx.rs[s]];
+    for (int s = 0; s < rx.np; ++s) Pp *= CS[rx.ps[s]];
+    double q;
+    if (rx.rev) {
+      double dG = -rx.dnu * lnP0RT;
+      for (int s = 0; s < rx.np; ++s) dG += GS[rx.ps[s]];
+      for (int s = 0; s < rx.nr; ++s) dG -= GS[rx.rs[s]];
+      const double kr = kf * pgb_exp64(fmin(dG, 700.0));  // finite: Pp = 0 gives 0, not NaN
+      q = fma(kf, Pf, -kr * Pp);
+    } else {
+      q = kf * Pf;
+    }
+    if (rx.kind == 1) q *= Mc;
+    QS[j] = q;
+  }
+  __syncwarp();
+  double hs = 0.0, rcp = 0.0;
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const int k = idx(r);
+    f[r] = 0.0;
+    if (k < NS) {
+      double wdot = 0.0;
+      const int e1 = Tab::sprx_end(k);
+      for (int e = Tab::sprx_begin(k); e < e1; ++e) wdot = fma(Tab::sprx_nu(e), QS[Tab::sprx_j(e)], wdot);
+      const TabSpecies<double>& s = Tab::template sp<double>(k);
+      const double wm = fma(wdot, s.W, FRC[k]);
+      f[r] = wm;
+      const bool lo = T < s.Tmid;
+      const double* a = lo ? s.lo : s.hi;
+      const double* hc = lo ? s.hlo : s.hhi;
+      const double hRT = fma(T, fma(T, fma(T, fma(T, hc[4], hc[3]), hc[2]), hc[1]), fma(hc[5], invT, hc[0]));
+      const double cpR = fma(T, fma(T, fma(T, fma(T, a[4], a[3]), a[2]), a[1]), a[0]);
+      hs = fma(hRT * s.invW, wm, hs);
+      rcp = fma(y[r] * s.invW, cpR, rcp);
+    }
+  }
+  hs = warp_sum(hs);
+  rcp = warp_sum(rcp);
+  const double fT = fma(-hs, kRerg * T, FRC[NS]) / (rcp * kRerg);
+#pragma unroll
+  for (int r = 0; r < R; ++r)
+    if (idx(r) == NS) f[r] = fT;
+  __syncwarp();  // CS/GS/QS are reused by the next evaluation
+  return fv;
+}
+
 template <class M, class JR, int WPB>
 __global__ void __launch_bounds__(WPB * 32, 1) bdf_warp_kernel(const ReactParams P) {
   using namespace bdf;
@@ -102,97 +219,12 @@ __global__ void __launch_bounds__(WPB * 32, 1) bdf_warp_kernel(const ReactParams
 
   // ---- right-hand side: f = [W_k wdot_k + F_k, dT/dt] at y ----
   auto rhs = [&](const double (&y)[R], double (&f)[R]) {
-    const double T = bcast(y, NS);
-    const double invT = 1.0 / T;
-    const double lnT = pgb_log64(T);
-    const double lnT1 = 1.0 - lnT;
-    const double lnP0RT = kLnP0OverR - lnT;
-    double c_loc = 0.0;
+    WVec<M> yv;
 #pragma unroll
-    for (int r = 0; r < R; ++r) {
-      const int k = idx(r);
-      if (k < NS) {
-        const TabSpecies<double>& s = Tab::template sp<double>(k);
-        const double c = y[r] * s.invW;
-        CS[k] = c;
-        c_loc += c;
-        const double* g = T < s.Tmid ? s.glo : s.ghi;
-        GS[k] = fma(g[0], lnT1, fma(T, fma(T, fma(T, fma(T, g[4], g[3]), g[2]), g[1]), fma(g[5], invT, g[6])));
-      }
-    }
-    const double Ctot = warp_sum(c_loc);
-    __syncwarp();
-    for (int j = lane; j < NR; j += 32) {
-      const TabReaction<double>& rx = Tab::template rx<double>(j);
-      const double lnkf = fma(rx.beta, lnT, fma(rx.mEaR, invT, rx.lnA));
-      double kf = pgb_exp64(lnkf);
-      double Mc = 1.0;
-      if (rx.tb >= 0) {
-        const TabThirdBody<double>& tb = Tab::template tb<double>(rx.tb);
-        Mc = Ctot;
-        for (int e = 0; e < tb.n; ++e) Mc = fma(tb.effm1[e], CS[tb.sp[e]], Mc);
-      }
-      if (rx.kind == 2) {
-        const TabTroe<double>& fo = Tab::template troe<double>(rx.troe);
-        const double lnk0 = fma(fo.beta0, lnT, fma(fo.mEa0R, invT, fo.lnA0));
-        const double Pr = Mc * pgb_exp64(lnk0 - lnkf);
-        double blend = Pr / (1.0 + Pr);
-        if (fo.ntroe > 0) {
-          double Fcent = fma(fo.one_m_a, pgb_exp64(T * fo.m_invT3), fo.a * pgb_exp64(T * fo.m_invT1));
-          if (fo.ntroe > 3) Fcent += pgb_exp64(invT * fo.m_T2);
-          const double lFc = pgb_log64(Fcent) * 0.4342944819032518;
-          const double cc = fma(-0.67, lFc, -0.4), nn = fma(-1.27, lFc, 0.75);
-          const double lPr = pgb_log64(fmax(Pr, 1e-300)) * 0.4342944819032518 + cc;
-          const double f1 = lPr / fma(-0.14, lPr, nn);
-          blend *= pgb_exp64(2.302585092994046 * lFc / fma(f1, f1, 1.0));
-        }
-        kf *= blend;
-      }
-      double Pf = 1.0, Pp = 1.0;
-      for (int s = 0; s < rx.nr; ++s) Pf *= CS[rx.rs[s]];
-      for (int s = 0; s < rx.np; ++s) Pp *= CS[rx.ps[s]];
-      double q;
-      if (rx.rev) {
-        double dG = -rx.dnu * lnP0RT;
-        for (int s = 0; s < rx.np; ++s) dG += GS[rx.ps[s]];
-        for (int s = 0; s < rx.nr; ++s) dG -= GS[rx.rs[s]];
-        const double kr = kf * pgb_exp64(fmin(dG, 700.0));  // finite: Pp = 0 gives 0, not NaN
-        q = fma(kf, Pf, -kr * Pp);
-      } else {
-        q = kf * Pf;
-      }
-      if (rx.kind == 1) q *= Mc;
-      QS[j] = q;
-    }
-    __syncwarp();
-    double hs = 0.0, rcp = 0.0;
+    for (int r = 0; r < R; ++r) yv.v[r] = y[r];
+    const WVec<M> fv = warp_rhs<M>(yv, CS, GS, QS, FRC);
 #pragma unroll
-    for (int r = 0; r < R; ++r) {
-      const int k = idx(r);
-      f[r] = 0.0;
-      if (k < NS) {
-        double wdot = 0.0;
-        const int e1 = Tab::sprx_end(k);
-        for (int e = Tab::sprx_begin(k); e < e1; ++e) wdot = fma(Tab::sprx_nu(e), QS[Tab::sprx_j(e)], wdot);
-        const TabSpecies<double>& s = Tab::template sp<double>(k);
-        const double wm = fma(wdot, s.W, FRC[k]);
-        f[r] = wm;
-        const bool lo = T < s.Tmid;
-        const double* a = lo ? s.lo : s.hi;
-        const double* hc = lo ? s.hlo : s.hhi;
-        const double hRT = fma(T, fma(T, fma(T, fma(T, hc[4], hc[3]), hc[2]), hc[1]), fma(hc[5], invT, hc[0]));
-        const double cpR = fma(T, fma(T, fma(T, fma(T, a[4], a[3]), a[2]), a[1]), a[0]);
-        hs = fma(hRT * s.invW, wm, hs);
-        rcp = fma(y[r] * s.invW, cpR, rcp);
-      }
-    }
-    hs = warp_sum(hs);
-    rcp = warp_sum(rcp);
-    const double fT = fma(-hs, kRerg * T, FRC[NS]) / (rcp * kRerg);
-#pragma unroll
-    for (int r = 0; r < R; ++r)
-      if (idx(r) == NS) f[r] = fT;
-    __syncwarp();  // CS/GS/QS are reused by the next evaluation
+    for (int r = 0; r < R; ++r) f[r] = fv.v[r];
   };
 
   // ---- analytic Jacobian into A (equations of jac_table, mech_tables.cuh), in type JR ----

@@ -280,10 +280,11 @@ LaunchPlan plan_launch(const pgb_reactor* r, long long ncell) {
     // warp per cell: as many warps per block as fit shared memory (or gb.wpb), one block per SM
     const int per = r->opt.mixed ? m.wsmem_mixed : m.wsmem_fp64;
     int wpb = r->opt.wpb;
-    if (wpb <= 0) {
-      wpb = 4;
-      for (int c : {16, 8, 6})
-        if (c * per <= kMaxSmemPerBlock) { wpb = c; break; }
+    if (wpb <= 0) {  // most preferred compiled size whose shared memory fits
+      for (int i = 0; i < 4 && m.wpb_choice[i] > 0; ++i) {
+        wpb = m.wpb_choice[i];
+        if (m.wpb_choice[i] * per <= kMaxSmemPerBlock) break;
+      }
     }
     pl.warp = true;
     pl.tpb = wpb;

@@ -72,7 +72,7 @@ int launch_bdf(const pgb::ReactParams& p, int tpb, cudaStream_t s, int nblocks) 
   }
 }
 
-// Warp-per-cell BDF: `wpb` warps per block (4, 6, 8 or 16), one persistent block per SM.
+// Warp-per-cell BDF: `wpb` warps per block, one persistent block per SM.
 template <class M, class JR, int WPB>
 int launch_bdf_warp_wpb(const pgb::ReactParams& p, cudaStream_t s, int nblocks) {
   constexpr int smem = WPB * pgb::bdf_warp_smem_per_warp<M, JR>();
@@ -88,15 +88,35 @@ int launch_bdf_warp_wpb(const pgb::ReactParams& p, cudaStream_t s, int nblocks) 
   }
 }
 
+// Warps per block compiled for a mechanism, most preferred first (0 ends the list): one size
+// for small mechanisms (the warp mapping is not their default), 16 for mid-sized ones (more
+// resident warps hide the latency of the lane-parallel RHS; 24 measured slower: the register
+// cap then spills), what shared memory allows for the large ones.
+template <class M>
+constexpr int warp_wpb_choice(int i) {
+  if constexpr (M::NS <= 12) {
+    return i == 0 ? 8 : 0;
+  } else if constexpr (M::N <= 32) {
+    constexpr int c[] = {16, 8, 0, 0};
+    return i < 4 ? c[i] : 0;
+  } else {
+    constexpr int c[] = {6, 4, 0, 0};
+    return i < 4 ? c[i] : 0;
+  }
+}
+
 template <class M, class JR>
 int launch_bdf_warp(const pgb::ReactParams& p, int wpb, cudaStream_t s, int nblocks) {
-  switch (wpb) {
-    case 4: return launch_bdf_warp_wpb<M, JR, 4>(p, s, nblocks);
-    case 6: return launch_bdf_warp_wpb<M, JR, 6>(p, s, nblocks);
-    case 8: return launch_bdf_warp_wpb<M, JR, 8>(p, s, nblocks);
-    case 16: return launch_bdf_warp_wpb<M, JR, 16>(p, s, nblocks);
-    default: return set_err("warp BDF: gb.wpb must be 4, 6, 8 or 16 (got %d)", wpb);
+  if constexpr (M::NS <= 12) {
+    if (wpb == 8) return launch_bdf_warp_wpb<M, JR, 8>(p, s, nblocks);
+  } else if constexpr (M::N <= 32) {
+    if (wpb == 16) return launch_bdf_warp_wpb<M, JR, 16>(p, s, nblocks);
+    if (wpb == 8) return launch_bdf_warp_wpb<M, JR, 8>(p, s, nblocks);
+  } else {
+    if (wpb == 6) return launch_bdf_warp_wpb<M, JR, 6>(p, s, nblocks);
+    if (wpb == 4) return launch_bdf_warp_wpb<M, JR, 4>(p, s, nblocks);
   }
+  return set_err("warp BDF: %d warps per block are not compiled for %s", wpb, M::NAME);
 }
 
 template <class M>
@@ -147,6 +167,7 @@ struct MechEntry {
   LaunchFn warp_mixed, warp_fp64;  // warp-per-cell BDF (argument: warps per block)
   int wsmem_mixed, wsmem_fp64;     // shared bytes per warp
   int (*sg_feat_fn)(const pgb::BoxDev*, int, long long, float*, cudaStream_t);
+  int wpb_choice[4];  // warps per block compiled for the warp kernel, preferred first, 0-ended
 };
 
 
@@ -224,7 +245,11 @@ int h2t_entry(const pgb_box_view* v, double tmin, double tmax, cudaStream_t s) {
         ::pgb_host::h2t_entry<M>, ::pgb_host::launch_surrogate<M>,                           \
         ::pgb_host::launch_surrogate_audit<M>, ::pgb_host::launch_bdf_warp<M, float>,        \
         ::pgb_host::launch_bdf_warp<M, double>, pgb::bdf_warp_smem_per_warp<M, float>(),     \
-        pgb::bdf_warp_smem_per_warp<M, double>(), ::pgb_host::launch_surrogate_features<M>   \
+        pgb::bdf_warp_smem_per_warp<M, double>(), ::pgb_host::launch_surrogate_features<M>,  \
+    {                                                                                        \
+      ::pgb_host::warp_wpb_choice<M>(0), ::pgb_host::warp_wpb_choice<M>(1),                  \
+          ::pgb_host::warp_wpb_choice<M>(2), ::pgb_host::warp_wpb_choice<M>(3)               \
+    }                                                                                        \
   }
 
 // Mechanisms too large for one cell per thread: warp-per-cell BDF, ReactorNull and T(h, Y) only.
@@ -234,7 +259,11 @@ int h2t_entry(const pgb_box_view* v, double tmin, double tmax, cudaStream_t s) {
         nullptr, ::pgb_host::h2t_entry<M>, nullptr, nullptr,                                 \
         ::pgb_host::launch_bdf_warp<M, float>, ::pgb_host::launch_bdf_warp<M, double>,       \
         pgb::bdf_warp_smem_per_warp<M, float>(), pgb::bdf_warp_smem_per_warp<M, double>(),   \
-        nullptr                                                                              \
+        nullptr,                                                                             \
+    {                                                                                        \
+      ::pgb_host::warp_wpb_choice<M>(0), ::pgb_host::warp_wpb_choice<M>(1),                  \
+          ::pgb_host::warp_wpb_choice<M>(2), ::pgb_host::warp_wpb_choice<M>(3)               \
+    }                                                                                        \
   }
 
 // Converts and validates one box view into its device descriptor; cell numbering of the box
