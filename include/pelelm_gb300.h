@@ -89,6 +89,20 @@ int pgb_reactor_react(pgb_reactor* r, const pgb_box_view* view, double* dt_react
 int pgb_reactor_react_boxes(pgb_reactor* r, const pgb_box_view* views, int nbox, double dt_react,
                             double time, void* stream);
 
+/* The whole chemistry step of PeleLM::advance_chemistry (Source/PeleLM.cpp:5626-5845) for all
+ * boxes in one launch, on the caller's MKS arrays: the MKS -> CGS scaling before react
+ * (:5736-5746), the advance, the CGS -> MKS scaling after it (:5763-5771) and the reaction
+ * source I_R = -(rhoY_old - rhoY_new) / dt - F_rhoY (:5801) are done inside the kernels' cell
+ * load and write-back, so the caller's separate passes and per-box synchronizations go away.
+ * rhoY [kg/m^3], rhoH [J/m^3], T [K] in/out; forcing in kg/m^3/s and W/m^3; FC out; mask
+ * optional (int, < 0: covered); I_R optional (NUM_SPECIES comps, kg/m^3/s; -F for covered cells).
+ * Plain BDF and ReactorNull; a reactor with gb.surrogate is refused (it takes CGS arrays). */
+typedef struct pgb_chem_view {
+  pgb_box box;
+  pgb_array4 rhoY, rhoY_src, T, rhoH, rhoH_src, FC, mask, I_R;
+} pgb_chem_view;
+int pgb_advance_chemistry(pgb_reactor* r, const pgb_chem_view* views, int nbox, double dt, void* stream);
+
 /* Waits for the last advance on its stream and returns its counters. */
 int pgb_reactor_get_stats(pgb_reactor* r, pgb_stats* out);
 
@@ -139,6 +153,13 @@ int pgb_version(void);
  * / FC fields are unused; rhoYdot goes to `out`. */
 int pgb_reaction_rates(const char* mechanism, const pgb_box_view* view, const pgb_array4* out,
                        void* stream);
+
+/* Heat release rate HR = -sum_k rhoYdot_k h_k(T) [W/m^3]: the HeatRelease derive
+ * (Source/PeleLM_derive.cpp:627-650, registered at Source/PeleLM_setup.cpp:838-840). MKS in:
+ * T [K] (1 comp), rhoYdot [kg/m^3/s] (NUM_SPECIES comps, the reaction source I_R); out: hr
+ * (1 comp). Arrays must cover the box. */
+int pgb_heat_release(const char* mechanism, const pgb_box* box, const pgb_array4* T,
+                     const pgb_array4* rhoYdot, const pgb_array4* hr, void* stream);
 
 /* T from (rho h, Y): the per-cell work of RhoH_to_Temp / getTfromHY (Source/PeleLM.cpp:8201-8287,
  * Source/PeleLM_K.H:508-529). MKS in: rhoY (view->rY), rhoH (view->rEner), T in/out (view->T).

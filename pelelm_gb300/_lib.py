@@ -28,6 +28,11 @@ class BoxView(C.Structure):
                 ("rEner", Array4), ("rEner_src", Array4), ("FC", Array4), ("mask", Array4)]
 
 
+class ChemView(C.Structure):
+    _fields_ = [("box", Box)] + [(n, Array4) for n in ("rhoY", "rhoY_src", "T", "rhoH", "rhoH_src", "FC", "mask",
+                                                        "I_R")]
+
+
 class Stats(C.Structure):
     _fields_ = [("ncell", C.c_ulonglong), ("nst", C.c_ulonglong), ("nfe", C.c_ulonglong),
                 ("nje", C.c_ulonglong), ("netf", C.c_ulonglong), ("ncfn", C.c_ulonglong),
@@ -54,6 +59,8 @@ EXPORTS = {
     "pgb_reactor_get_surrogate_stats": (C.c_int, [_vp, C.POINTER(SurrogateStats)]),
     "pgb_surrogate_features": (C.c_int, [C.c_char_p, _vp, C.c_int, _vp, _vp]),
     "pgb_reactor_surrogate_raw": (C.c_int, [_vp, _vp, C.c_int, _vp, _vp, _vp]),
+    "pgb_heat_release": (C.c_int, [C.c_char_p, _vp, _vp, _vp, _vp, _vp]),
+    "pgb_advance_chemistry": (C.c_int, [_vp, _vp, C.c_int, C.c_double, _vp]),
     "pgb_reactor_close": (None, [_vp]),
     "pgb_reaction_rates": (C.c_int, [C.c_char_p, C.POINTER(BoxView), C.POINTER(Array4), _vp]),
     "pgb_rhoh_to_temp": (C.c_int, [C.c_char_p, C.POINTER(BoxView), C.c_double, C.c_double, _vp]),

@@ -356,10 +356,17 @@ __global__ void __launch_bounds__(TPB, 1) bdf_reactor_kernel(const ReactParams P
       Tn = fmax(90.0, fmin(5000.0, Tn + dT));
       if (fabs(dT) < 1e-10 * Tn) break;
     }
+    if (B.IR.p) {
+      const double dt_inv = 1.0 / tout;
 #pragma unroll
-    for (int k = 0; k < NS; ++k) elem(B.rY, k) = Z(0, k);
+      for (int k = 0; k < NS; ++k)  // separate roundings, as separate passes over arrays give
+        elem(B.IR, k) = __dsub_rn(__dmul_rn(-__dsub_rn(elem(B.rY, k), __dmul_rn(Z(0, k), B.sY_out)), dt_inv),
+                                  elem(B.rYsrc, k));
+    }
+#pragma unroll
+    for (int k = 0; k < NS; ++k) elem(B.rY, k) = Z(0, k) * B.sY_out;
     elem(B.T, 0) = Tn;
-    elem(B.rE, 0) = rE;
+    elem(B.rE, 0) = rE * B.sE_out;
     elem(B.FC, 0) = (status == OK) ? (double)nfe : -(double)status;
     ReactStats* S = P.stats;
     atomicAdd(&S->nst, (unsigned long long)nst);
@@ -397,17 +404,19 @@ __global__ void __launch_bounds__(TPB, 1) bdf_reactor_kernel(const ReactParams P
                               (long long)(ck - B.mask.begin2) * B.mask.kstride];
       if (mv < 0) {  // covered cell: no reaction, zero function count
         elem(B.FC, 0) = 0.0;
+        if (B.IR.p)
+          for (int k = 0; k < NS; ++k) elem(B.IR, k) = -elem(B.rYsrc, k);
         return false;
       }
     }
 #pragma unroll
     for (int k = 0; k < NS; ++k) {
-      Z(0, k) = elem(B.rY, k);
-      FRC(k) = elem(B.rYsrc, k);
+      Z(0, k) = elem(B.rY, k) * B.sY_in;
+      FRC(k) = elem(B.rYsrc, k) * B.sY_in;
     }
     Z(0, NS) = elem(B.T, 0);
-    FRC(NS) = elem(B.rEsrc, 0);
-    rE0 = elem(B.rE, 0);
+    FRC(NS) = elem(B.rEsrc, 0) * B.sE_in;
+    rE0 = elem(B.rE, 0) * B.sE_in;
     for (int j = 1; j <= QMAX + 1; ++j)
 #pragma unroll
       for (int i = 0; i < N; ++i) Z(j, i) = 0.0;

@@ -519,6 +519,8 @@ __global__ void __launch_bounds__(WPB * 32, 1) bdf_warp_kernel(const ReactParams
     if (B.mask.p && B.mask.p[(long long)(ci - B.mask.begin0) + (long long)(cj - B.mask.begin1) * B.mask.jstride +
                              (long long)(ck - B.mask.begin2) * B.mask.kstride] < 0) {
       if (lane == 0) elem(B.FC, 0) = 0.0;
+      if (B.IR.p)
+        for (int k = lane; k < NS; k += 32) elem(B.IR, k) = -elem(B.rYsrc, k);
       continue;
     }
     double y[R], f[R], acor[R], tmp[R], acor_saved[R];
@@ -526,11 +528,11 @@ __global__ void __launch_bounds__(WPB * 32, 1) bdf_warp_kernel(const ReactParams
     for (int r = 0; r < R; ++r) {
       const int i = idx(r);
       y[r] = 0.0; f[r] = 0.0; acor[r] = 0.0; tmp[r] = 0.0; acor_saved[r] = 0.0; ewt[r] = 1.0;
-      if (i < NS) { y[r] = elem(B.rY, i); FRC[i] = elem(B.rYsrc, i); }
-      else if (i == NS) { y[r] = elem(B.T, 0); FRC[NS] = elem(B.rEsrc, 0); }
+      if (i < NS) { y[r] = elem(B.rY, i) * B.sY_in; FRC[i] = elem(B.rYsrc, i) * B.sY_in; }
+      else if (i == NS) { y[r] = elem(B.T, 0); FRC[NS] = elem(B.rEsrc, 0) * B.sE_in; }
       if (i < N) Z[i] = y[r];
     }
-    const double rE0 = elem(B.rE, 0);
+    const double rE0 = elem(B.rE, 0) * B.sE_in;
     if (lane < QMAX + 2) TAU[lane] = 0.0;
     __syncwarp();
     auto zget = [&](int j, int r) -> double& { return Z[j * N + idx(r)]; };
@@ -957,10 +959,16 @@ __global__ void __launch_bounds__(WPB * 32, 1) bdf_warp_kernel(const ReactParams
     }
 #pragma unroll
     for (int r = 0; r < R; ++r)
-      if (idx(r) < NS) elem(B.rY, idx(r)) = zget(0, r);
+      if (idx(r) < NS) {
+        const double rYn = __dmul_rn(zget(0, r), B.sY_out);
+        if (B.IR.p)  // separate roundings, as separate passes over arrays give
+          elem(B.IR, idx(r)) = __dsub_rn(__dmul_rn(-__dsub_rn(elem(B.rY, idx(r)), rYn), 1.0 / tout),
+                                         elem(B.rYsrc, idx(r)));
+        elem(B.rY, idx(r)) = rYn;
+      }
     if (lane == 0) {
       elem(B.T, 0) = Tn;
-      elem(B.rE, 0) = rE;
+      elem(B.rE, 0) = rE * B.sE_out;
       elem(B.FC, 0) = (status == OK) ? (double)nfe : -(double)status;
       ReactStats* S = P.stats;
       atomicAdd(&S->nst, (unsigned long long)nst);

@@ -6,6 +6,7 @@
 #define PGB_POINT_KERNELS_CUH
 
 #include "mech_common.cuh"
+#include "mech_tables.cuh"
 #include "reactor_types.cuh"
 
 namespace pgb {
@@ -92,6 +93,31 @@ __global__ void h2t_kernel(const PointParams p) {
   T = hy2t_newton<M>(arr_at(p.rE, i, j, k, 0) * inv_rho * 1.0e4, Y, T, p.tmin, p.tmax);
 }
 
+// Heat release rate -sum_k rhoYdot_k h_k(T) [W/m^3] from T and the MKS reaction rates
+// rhoYdot [kg/m^3/s] (p.rY), h_k from the NASA-7 tables (erg/g, times 1e-4 -> J/kg); the
+// per-cell work of the HeatRelease derive (Source/PeleLM_derive.cpp:627-650).
+template <class M>
+__global__ void heat_release_kernel(const PointParams p) {
+  using Tab = typename M::TabG;
+  const long long n = (long long)p.len0 * p.len1 * p.len2;
+  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n) return;
+  const int i = p.lo0 + (int)(c % p.len0);
+  const int j = p.lo1 + (int)((c / p.len0) % p.len1);
+  const int k = p.lo2 + (int)(c / ((long long)p.len0 * p.len1));
+  const double T = arr_at(p.T, i, j, k, 0);
+  const double invT = 1.0 / T;
+  double hr = 0.0;
+  for (int s = 0; s < M::NS; ++s) {
+    const TabSpecies<double>& sp = Tab::template sp<double>(s);
+    const double* hc = T < sp.Tmid ? sp.hlo : sp.hhi;
+    const double hRT = fma(T, fma(T, fma(T, fma(T, hc[4], hc[3]), hc[2]), hc[1]), fma(hc[5], invT, hc[0]));
+    const double h_mks = hRT * kRerg * T * sp.invW * 1.0e-4;  // erg/g -> J/kg
+    hr = fma(-arr_at(p.rY, i, j, k, s), h_mks, hr);
+  }
+  arr_at(p.out, i, j, k, 0) = hr;
+}
+
 // ReactorNull: rhoY += dt F, rho h += dt F_h, T from the new (h, Y), FC = 0 (CGS, in place).
 template <class M>
 __global__ void null_reactor_kernel(const ReactParams P) {
@@ -111,24 +137,34 @@ __global__ void null_reactor_kernel(const ReactParams P) {
     if (B.mask.p) {
       const int mv = B.mask.p[(long long)(i - B.mask.begin0) + (long long)(j - B.mask.begin1) * B.mask.jstride +
                               (long long)(k - B.mask.begin2) * B.mask.kstride];
-      if (mv < 0) { arr_at(B.FC, i, j, k, 0) = 0.0; continue; }
+      if (mv < 0) {
+        arr_at(B.FC, i, j, k, 0) = 0.0;
+        if (B.IR.p)
+          for (int s = 0; s < M::NS; ++s) arr_at(B.IR, i, j, k, s) = -arr_at(B.rYsrc, i, j, k, s);
+        continue;
+      }
     }
     double Y[M::NS];
     double rho = 0.0;
 #pragma unroll
     for (int s = 0; s < M::NS; ++s) {
       double& v = arr_at(B.rY, i, j, k, s);
-      v = fma(P.dt, arr_at(B.rYsrc, i, j, k, s), v);
-      Y[s] = v;
-      rho += v;
+      const double vn = fma(P.dt, arr_at(B.rYsrc, i, j, k, s) * B.sY_in, v * B.sY_in);  // CGS
+      const double vo = __dmul_rn(vn, B.sY_out);
+      if (B.IR.p)
+        arr_at(B.IR, i, j, k, s) = __dsub_rn(__dmul_rn(-__dsub_rn(v, vo), 1.0 / P.dt), arr_at(B.rYsrc, i, j, k, s));
+      v = vo;
+      Y[s] = vn;
+      rho += vn;
     }
     double& rE = arr_at(B.rE, i, j, k, 0);
-    rE = fma(P.dt, arr_at(B.rEsrc, i, j, k, 0), rE);
+    const double rEn = fma(P.dt, arr_at(B.rEsrc, i, j, k, 0) * B.sE_in, rE * B.sE_in);  // CGS
+    rE = rEn * B.sE_out;
     const double inv_rho = 1.0 / rho;
 #pragma unroll
     for (int s = 0; s < M::NS; ++s) Y[s] *= inv_rho;
     double& T = arr_at(B.T, i, j, k, 0);
-    T = hy2t_newton<M>(rE * inv_rho, Y, T, 90.0, 5000.0);
+    T = hy2t_newton<M>(rEn * inv_rho, Y, T, 90.0, 5000.0);
     arr_at(B.FC, i, j, k, 0) = 0.0;
   }
 }

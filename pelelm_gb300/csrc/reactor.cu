@@ -147,6 +147,8 @@ int build_boxes(const pgb_box_view* v, int nbox, int ns, std::vector<pgb::BoxDev
       return -1;
     if (v[b].mask.p && check_arr(v[b].mask, bx, 1, "mask", b)) return -1;
     pgb::BoxDev& d = out[b];
+    std::memset(&d, 0, sizeof(d));  // also the padding: the graph cache compares box tables bytewise
+    d.sY_in = d.sE_in = d.sY_out = d.sE_out = 1.0;
     d.lo0 = bx.lo[0]; d.lo1 = bx.lo[1]; d.lo2 = bx.lo[2];
     d.len0 = bx.hi[0] - bx.lo[0] + 1;
     d.len1 = bx.hi[1] - bx.lo[1] + 1;
@@ -492,19 +494,17 @@ int pgb_reactor_set_typ_vals_ode(pgb_reactor* r, const double* typ, int n) {
   return 0;
 }
 
-int pgb_reactor_react_boxes(pgb_reactor* r, const pgb_box_view* views, int nbox, double dt_react,
-                            double time, void* stream) {
-  (void)time;
-  if (!r) return set_err("null reactor");
-  if (nbox < 0 || (nbox > 0 && !views)) return set_err("bad box list");
-  if (!(dt_react > 0.0)) return set_err("dt_react must be > 0");
-  cudaStream_t st = static_cast<cudaStream_t>(stream);
-  std::lock_guard<std::mutex> g(r->mu);
+}  // extern "C"
+
+namespace {
+
+// Enqueues one advance of the prepared box table on `st` (a captured graph is replayed when the
+// box table and dt repeat); the caller holds r->mu.
+int advance_box_table(pgb_reactor* r, const std::vector<pgb::BoxDev>& boxes, long long ncell, double dt_react,
+                      cudaStream_t st) {
+  const int nbox = (int)boxes.size();
   Scratch* s = nullptr;
   if (ensure_scratch(r, st, std::max(nbox, 1), &s)) return -1;
-  std::vector<pgb::BoxDev> boxes;
-  long long ncell = 0;
-  if (build_boxes(views, nbox, r->mech->ns, boxes, ncell)) return -1;
   if (!r->null_reactor) {
     const LaunchPlan pl = plan_launch(r, ncell);
     if (ensure_buf(*s, s->d_z, s->z_cap, pl.z_bytes) || ensure_buf(*s, s->d_lu, s->lu_cap, pl.lu_bytes))
@@ -541,6 +541,52 @@ int pgb_reactor_react_boxes(pgb_reactor* r, const pgb_box_view* views, int nbox,
   }
   PGB_CUDA(cudaEventRecord(s->done, st));
   return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pgb_reactor_react_boxes(pgb_reactor* r, const pgb_box_view* views, int nbox, double dt_react,
+                            double time, void* stream) {
+  (void)time;
+  if (!r) return set_err("null reactor");
+  if (nbox < 0 || (nbox > 0 && !views)) return set_err("bad box list");
+  if (!(dt_react > 0.0)) return set_err("dt_react must be > 0");
+  std::lock_guard<std::mutex> g(r->mu);
+  std::vector<pgb::BoxDev> boxes;
+  long long ncell = 0;
+  if (build_boxes(views, nbox, r->mech->ns, boxes, ncell)) return -1;
+  return advance_box_table(r, boxes, ncell, dt_react, static_cast<cudaStream_t>(stream));
+}
+
+int pgb_advance_chemistry(pgb_reactor* r, const pgb_chem_view* views, int nbox, double dt, void* stream) {
+  if (!r) return set_err("null reactor");
+  if (nbox < 0 || (nbox > 0 && !views)) return set_err("bad box list");
+  if (!(dt > 0.0)) return set_err("dt must be > 0");
+  if (r->sg.d_net) return set_err("advance_chemistry: the surrogate path takes CGS arrays (react_boxes)");
+  std::vector<pgb_box_view> bv(nbox);
+  for (int b = 0; b < nbox; ++b) {
+    const pgb_chem_view& c = views[b];
+    pgb_box_view& v = bv[b];
+    std::memset(&v, 0, sizeof(v));
+    v.box = c.box;
+    v.rY = c.rhoY; v.rY_src = c.rhoY_src; v.T = c.T; v.rEner = c.rhoH; v.rEner_src = c.rhoH_src;
+    v.FC = c.FC; v.mask = c.mask;
+    if (c.I_R.p && check_arr(c.I_R, c.box, r->mech->ns, "I_R", b)) return -1;
+  }
+  std::lock_guard<std::mutex> g(r->mu);
+  std::vector<pgb::BoxDev> boxes;
+  long long ncell = 0;
+  if (build_boxes(bv.data(), nbox, r->mech->ns, boxes, ncell)) return -1;
+  for (int b = 0; b < nbox; ++b) {  // MKS <-> CGS as advance_chemistry does (Source/PeleLM.cpp:5736-5771)
+    boxes[b].sY_in = 1.0e-3;
+    boxes[b].sE_in = 10.0;
+    boxes[b].sY_out = 1.0e3;
+    boxes[b].sE_out = 0.1;
+    if (views[b].I_R.p) boxes[b].IR = arr_dev(views[b].I_R);
+  }
+  return advance_box_table(r, boxes, ncell, dt, static_cast<cudaStream_t>(stream));
 }
 
 int pgb_reactor_get_stats(pgb_reactor* r, pgb_stats* out) {
@@ -662,6 +708,16 @@ int pgb_reaction_rates(const char* mechanism, const pgb_box_view* view, const pg
   if (!view || !out) return set_err("null argument");
   if (!m->rates_fn) return set_err("pointwise rates are not compiled for mechanism '%s'", m->name);
   return m->rates_fn(view, out, static_cast<cudaStream_t>(stream));
+}
+
+int pgb_heat_release(const char* mechanism, const pgb_box* box, const pgb_array4* T,
+                     const pgb_array4* rhoYdot, const pgb_array4* hr, void* stream) {
+  const MechEntry* m = find_mech(mechanism);
+  if (!m) return set_err("unknown mechanism '%s'", mechanism ? mechanism : "(null)");
+  if (!box || !T || !rhoYdot || !hr) return set_err("null argument");
+  for (int d = 0; d < 3; ++d)
+    if (box->hi[d] < box->lo[d]) return set_err("heat_release: empty box");
+  return m->hr_fn(box, T, rhoYdot, hr, static_cast<cudaStream_t>(stream));
 }
 
 int pgb_rhoh_to_temp(const char* mechanism, const pgb_box_view* view, double tmin, double tmax,

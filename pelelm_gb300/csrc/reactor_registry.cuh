@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstring>
 
 #include "../../include/pelelm_gb300.h"
 #include "bdf_kernel.cuh"
@@ -168,6 +169,7 @@ struct MechEntry {
   int wsmem_mixed, wsmem_fp64;     // shared bytes per warp
   int (*sg_feat_fn)(const pgb::BoxDev*, int, long long, float*, cudaStream_t);
   int wpb_choice[4];  // warps per block compiled for the warp kernel, preferred first, 0-ended
+  int (*hr_fn)(const pgb_box*, const pgb_array4*, const pgb_array4*, const pgb_array4*, cudaStream_t);
 };
 
 
@@ -216,6 +218,24 @@ int rates_entry(const pgb_box_view* v, const pgb_array4* out, cudaStream_t s) {
 }
 
 template <class M>
+int heat_release_entry(const pgb_box* b, const pgb_array4* T, const pgb_array4* rhoYdot, const pgb_array4* hr,
+                       cudaStream_t s) {
+  if (check_arr(*T, *b, 1, "T", 0) || check_arr(*rhoYdot, *b, M::NS, "rhoYdot", 0) ||
+      check_arr(*hr, *b, 1, "hr", 0))
+    return -1;
+  pgb::PointParams p;
+  std::memset(&p, 0, sizeof(p));
+  p.lo0 = b->lo[0]; p.lo1 = b->lo[1]; p.lo2 = b->lo[2];
+  p.len0 = b->hi[0] - b->lo[0] + 1; p.len1 = b->hi[1] - b->lo[1] + 1; p.len2 = b->hi[2] - b->lo[2] + 1;
+  p.T = arr_dev(*T); p.rY = arr_dev(*rhoYdot); p.out = arr_dev(*hr);
+  const long long n = (long long)p.len0 * p.len1 * p.len2;
+  if (n <= 0) return 0;
+  pgb::heat_release_kernel<M><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(p);
+  PGB_CUDA(cudaGetLastError());
+  return 0;
+}
+
+template <class M>
 int h2t_entry(const pgb_box_view* v, double tmin, double tmax, cudaStream_t s) {
   const pgb_box& b = v->box;
   if (check_arr(v->rY, b, M::NS, "rY", 0) || check_arr(v->T, b, 1, "T", 0) ||
@@ -250,6 +270,7 @@ int h2t_entry(const pgb_box_view* v, double tmin, double tmax, cudaStream_t s) {
       ::pgb_host::warp_wpb_choice<M>(0), ::pgb_host::warp_wpb_choice<M>(1),                  \
           ::pgb_host::warp_wpb_choice<M>(2), ::pgb_host::warp_wpb_choice<M>(3)               \
     }                                                                                        \
+    , ::pgb_host::heat_release_entry<M>                                                      \
   }
 
 // Mechanisms too large for one cell per thread: warp-per-cell BDF, ReactorNull and T(h, Y) only.
@@ -264,6 +285,7 @@ int h2t_entry(const pgb_box_view* v, double tmin, double tmax, cudaStream_t s) {
       ::pgb_host::warp_wpb_choice<M>(0), ::pgb_host::warp_wpb_choice<M>(1),                  \
           ::pgb_host::warp_wpb_choice<M>(2), ::pgb_host::warp_wpb_choice<M>(3)               \
     }                                                                                        \
+    , ::pgb_host::heat_release_entry<M>                                                      \
   }
 
 // Converts and validates one box view into its device descriptor; cell numbering of the box
@@ -278,6 +300,8 @@ inline int fill_box_dev(const pgb_box_view& v, int ns, long long cell_offset, in
       check_arr(v.rEner_src, bx, 1, "rEner_src", ibox) || check_arr(v.FC, bx, 1, "FC", ibox))
     return -1;
   if (v.mask.p && check_arr(v.mask, bx, 1, "mask", ibox)) return -1;
+  std::memset(&d, 0, sizeof(d));
+  d.sY_in = d.sE_in = d.sY_out = d.sE_out = 1.0;
   d.lo0 = bx.lo[0]; d.lo1 = bx.lo[1]; d.lo2 = bx.lo[2];
   d.len0 = bx.hi[0] - bx.lo[0] + 1;
   d.len1 = bx.hi[1] - bx.lo[1] + 1;

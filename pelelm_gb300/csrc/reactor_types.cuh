@@ -31,6 +31,11 @@ struct BoxDev {
   long long cell_offset;
   ArrDev rY, rYsrc, T, rE, rEsrc, FC;
   MaskDev mask;  // p may be null: all cells active
+  // Units of the caller's arrays: rhoY and its forcing are multiplied by sY_in and rho h and
+  // its forcing by sE_in when a cell is loaded, results by sY_out / sE_out when it is written
+  // (1 for CGS arrays; 1e-3, 10 / 1e3, 0.1 for PeleLM's MKS state, Source/PeleLM.cpp:5736-5771).
+  double sY_in, sE_in, sY_out, sE_out;
+  ArrDev IR;  // p may be null; else I_R = -(rhoY_old - rhoY_new) / dt - F_rhoY in the caller's units
 };
 
 // Per-launch counters (device scratch, zeroed before each launch).

@@ -128,6 +128,25 @@ class ReactorGB:
         check(lib().pgb_reactor_get_surrogate_stats(self._h, C.byref(s)), "get_surrogate_stats")
         return {n: getattr(s, n) for n, _ in _lib.SurrogateStats._fields_}
 
+    def advance_chemistry(self, boxes: List[BoxArrays], dt: float, I_R=None, stream=None) -> None:
+        """PeleLM's chemistry step on MKS arrays (rhoY kg/m^3, rhoH J/m^3, forcing kg/m^3/s and
+        W/m^3): scaling, advance, back-scaling and the reaction source I_R (optional list of
+        (NUM_SPECIES, nz, ny, nx) tensors, one per box) in one launch."""
+        views = []
+        for b, box in enumerate(boxes):
+            v = _lib.ChemView()
+            lo = box.box[0]
+            for d in range(3):
+                v.box.lo[d], v.box.hi[d] = box.box[0][d], box.box[1][d]
+            v.rhoY, v.rhoY_src, v.T = array4(box.rY, lo), array4(box.rY_src, lo), array4(box.T, lo)
+            v.rhoH, v.rhoH_src, v.FC = array4(box.rEner, lo), array4(box.rEner_src, lo), array4(box.FC, lo)
+            v.mask = array4(box.mask, lo) if box.mask is not None else _lib.Array4()
+            v.I_R = array4(I_R[b], lo) if I_R is not None else _lib.Array4()
+            views.append(v)
+        arr = (_lib.ChemView * len(views))(*views)
+        check(lib().pgb_advance_chemistry(self._h, arr, len(views), float(dt), _stream_ptr(stream)),
+              "advance_chemistry")
+
     def surrogate_raw(self, boxes: List[BoxArrays], out, in_rows=None) -> None:
         """Raw ensemble outputs [cell][member][n_out] (FP32 device tensor `out`) of the fused
         inference kernel, optionally its input rows [cell][k_in]; the boxes are not modified."""
@@ -173,3 +192,14 @@ def rhoh_to_temp(mechanism: str, box: Box, rhoY, rhoH, T, tmin=90.0, tmax=5000.0
     v = BoxArrays(box, rhoY, None, T, rhoH, None, None, None).view()
     check(lib().pgb_rhoh_to_temp(mechanism.encode(), C.byref(v), float(tmin), float(tmax),
                                  _stream_ptr(stream)), "rhoh_to_temp")
+
+
+def heat_release(mechanism: str, box: Box, T, rhoYdot, out, stream=None) -> None:
+    """HeatRelease derive over a box (MKS): out = -sum_k rhoYdot_k h_k(T) [W/m^3]."""
+    from ._lib import Box as CBox
+    b = CBox()
+    for d in range(3):
+        b.lo[d], b.hi[d] = box[0][d], box[1][d]
+    check(lib().pgb_heat_release(mechanism.encode(), C.byref(b), C.byref(array4(T, box[0])),
+                                 C.byref(array4(rhoYdot, box[0])), C.byref(array4(out, box[0])),
+                                 _stream_ptr(stream)), "heat_release")

@@ -53,3 +53,26 @@ def test_rhoh_to_temp_roundtrip(native_lib, cuda):
     rhoh_to_temp("lidryer_syn", box, rY, rE, Tg, 200.0, 4000.0)
     torch.cuda.synchronize()
     np.testing.assert_allclose(Tg.cpu().numpy().reshape(-1), cs.T, rtol=1e-9)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mech", ["lidryer_syn", "drm19_syn", "gri_syn"])
+def test_heat_release_matches_numpy(native_lib, cuda, mech):
+    """HeatRelease derive: -sum_k rhoYdot_k h_k(T) in W/m^3 (h_k in J/kg)."""
+    import numpy as np
+    from pelelm_gb300.reactor import heat_release
+    from pelelm_gb300.workloads import load_mechanism, species_h_mass
+    torch = cuda
+    m = load_mechanism(mech)
+    rng = np.random.default_rng(4)
+    nx, ny, nz = 9, 5, 3
+    T = rng.uniform(300.0, 2800.0, (nz, ny, nx))
+    wdot = rng.normal(0.0, 50.0, (m.ns, nz, ny, nx))
+    ref = -np.einsum("kzyx,zyxk->zyx", wdot, species_h_mass(m, T.reshape(-1)).reshape(nz, ny, nx, m.ns) * 1e-4)
+    Tt = torch.tensor(T[None], device="cuda")
+    wt = torch.tensor(wdot, device="cuda")
+    out = torch.zeros(1, nz, ny, nx, dtype=torch.float64, device="cuda")
+    lo = (2, -1, 7)
+    heat_release(mech, (lo, (lo[0] + nx - 1, lo[1] + ny - 1, lo[2] + nz - 1)), Tt, wt, out)
+    torch.cuda.synchronize()
+    np.testing.assert_allclose(out[0].cpu().numpy(), ref, rtol=1e-11, atol=1e-9 * np.abs(ref).max())

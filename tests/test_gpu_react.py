@@ -172,3 +172,43 @@ def test_null_reactor(native_lib, cuda):
     np.testing.assert_allclose(rEg, cs.rE + cfg.dt * cs.rEsrc, rtol=1e-14)
     assert np.all(FCg == 0)
     r.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mapping", ["thread", "warp"])
+def test_advance_chemistry_mks_matches_cgs_react_and_reference_passes(native_lib, cuda, mapping):
+    """pgb_advance_chemistry on MKS arrays (scaling, advance, back-scaling, I_R in the kernels)
+    against the caller's own passes around react_boxes, as advance_chemistry does them
+    (Source/PeleLM.cpp:5736-5801): rhoY *= 1e-3, rhoH *= 10 (and their forcing), react, rhoY *=
+    1e3, rhoH *= 0.1, I_R = -(rhoY_old - rhoY_new) / dt - F. Same arithmetic: bit for bit."""
+    torch = cuda
+    cfg = CONFIGS["lidryer_amr120"]
+    n = 4096
+    cs = make_cells(cfg, n, seed=17)
+    rng = np.random.default_rng(2)
+    cs.mask[:] = np.where(rng.uniform(size=n) < 0.05, -1, 1)
+    mks = make_cells(cfg, n, seed=17)  # the same state in MKS units
+    mks.rY, mks.rYsrc, mks.rE, mks.rEsrc = cs.rY * 1e3, cs.rYsrc * 1e3, cs.rE * 0.1, cs.rEsrc * 0.1
+    mks.mask[:] = cs.mask
+    opts = f"ode.rtol={cfg.rtol} ode.atol={cfg.atol} gb.mapping={mapping}"
+    # (a) caller's passes around the CGS react
+    a = boxes_from_cells(torch, mks, [16], with_mask=True)[0]
+    old = a.rY.clone()
+    a.rY.mul_(1.0e-3); a.rY_src.mul_(1.0e-3); a.rEner.mul_(10.0); a.rEner_src.mul_(10.0)
+    r = ReactorBase.create("ReactorCvode", cfg.mech, opts)
+    r.init(2, 1)
+    r.react_boxes([a], cfg.dt, 0.0)
+    a.rY.mul_(1.0e3); a.rEner.mul_(0.1)
+    src = torch.tensor(np.ascontiguousarray(mks.rYsrc.T.reshape(a.rY.shape)), device="cuda")
+    IR_a = -(old - a.rY) * (1.0 / cfg.dt) - src
+    # (b) fused
+    b = boxes_from_cells(torch, mks, [16], with_mask=True)[0]
+    IR_b = torch.zeros_like(b.rY)
+    r.advance_chemistry([b], cfg.dt, I_R=[IR_b])
+    torch.cuda.synchronize()
+    r.close()
+    for x, y in ((a.rY, b.rY), (a.T, b.T), (a.rEner, b.rEner), (a.FC, b.FC)):
+        assert torch.equal(x, y)
+    cov = torch.tensor(cs.mask.reshape(16, 16, 16) < 0, device="cuda")
+    assert torch.equal(IR_a[:, ~cov], IR_b[:, ~cov])
+    assert torch.equal(IR_b[:, cov], -src[:, cov])
