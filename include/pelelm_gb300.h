@@ -95,7 +95,8 @@ int pgb_reactor_react_boxes(pgb_reactor* r, const pgb_box_view* views, int nbox,
  * source I_R = -(rhoY_old - rhoY_new) / dt - F_rhoY (:5801) are done inside the kernels' cell
  * load and write-back, so the caller's separate passes and per-box synchronizations go away.
  * rhoY [kg/m^3], rhoH [J/m^3], T [K] in/out; forcing in kg/m^3/s and W/m^3; FC out; mask
- * optional (int, < 0: covered); I_R optional (NUM_SPECIES comps, kg/m^3/s; -F for covered cells).
+ * optional (int, < 0: covered; their state is left untouched); I_R optional (NUM_SPECIES comps,
+ * kg/m^3/s; -F for covered cells).
  * Plain BDF and ReactorNull; a reactor with gb.surrogate is refused (it takes CGS arrays). */
 typedef struct pgb_chem_view {
   pgb_box box;

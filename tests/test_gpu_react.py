@@ -207,8 +207,13 @@ def test_advance_chemistry_mks_matches_cgs_react_and_reference_passes(native_lib
     r.advance_chemistry([b], cfg.dt, I_R=[IR_b])
     torch.cuda.synchronize()
     r.close()
-    for x, y in ((a.rY, b.rY), (a.T, b.T), (a.rEner, b.rEner), (a.FC, b.FC)):
-        assert torch.equal(x, y)
     cov = torch.tensor(cs.mask.reshape(16, 16, 16) < 0, device="cuda")
+    for x, y in ((a.rY, b.rY), (a.T, b.T), (a.rEner, b.rEner), (a.FC, b.FC)):
+        assert torch.equal(x[:, ~cov], y[:, ~cov])
+    # covered cells: the fused path leaves the caller's values untouched (the caller's passes
+    # scale them down and up, x * 1e-3 * 1e3, which need not round-trip exactly)
+    b0 = boxes_from_cells(torch, mks, [16], with_mask=True)[0]
+    for x, y in ((b0.rY, b.rY), (b0.T, b.T), (b0.rEner, b.rEner)):
+        assert torch.equal(x[:, cov], y[:, cov])
     assert torch.equal(IR_a[:, ~cov], IR_b[:, ~cov])
     assert torch.equal(IR_b[:, cov], -src[:, cov])
