@@ -82,6 +82,7 @@ def main():
     print(json.dumps({"config": args.config, "cells": args.cells, "precision": args.precision,
                       "ms": times, "cells_per_s": args.cells / (min(times) / 1e3),
                       "nfe_per_cell": st["nfe"] / args.cells, "nst_per_cell": st["nst"] / args.cells,
+                      "nje_per_cell": st["nje"] / args.cells,
                       "nfail": st["nfail"]}))
 
 
