@@ -176,58 +176,21 @@ __device__ __noinline__ WVec<M> warp_rhs(const WVec<M> yv, double* CS, double* G
   return fv;
 }
 
-template <class M, class JR, int WPB>
-__global__ void __launch_bounds__(WPB * 32, 1) bdf_warp_kernel(const ReactParams P) {
-  using namespace bdf;
+// Jacobian (equations of jac_table, mech_tables.cuh) and partial-pivot LU of I - gamma J in
+// shared memory, one warp cooperating; out of line like warp_rhs (called every few steps,
+// it would otherwise share the instruction cache with the step loop). False: singular.
+template <class M, class JR>
+__device__ __noinline__ bool warp_setup(const WVec<M> yv, const double gamma, const double* FRC, JR* A,
+                                        JR* XS, JR* RX, int* PIV) {
   using Tab = typename M::TabG;
   constexpr int N = M::N, NS = M::NS, NR = M::NR;
-  constexpr int R = (N + 31) / 32;   // vector elements per lane
-  constexpr int LDA = N + 1;         // padded matrix row
-  constexpr bool MIXED = sizeof(JR) == sizeof(float);
-  extern __shared__ __align__(16) unsigned char wsmem[];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  unsigned char* base = wsmem + (size_t)wid * bdf_warp_smem_per_warp<M, JR>();
-  double* Z = reinterpret_cast<double*>(base);   // [(QMAX+2)][N]
-  double* FRC = Z + (QMAX + 2) * N;              // [N] forcing (rhoY, then rho h)
-  double* CS = FRC + N;                          // [NS] concentrations
-  double* GS = CS + NS;                          // [NS] g/RT
-  double* QS = GS + NS;                          // [NR] rates of progress
-  double* LC = QS + NR;                          // [QMAX+1] l coefficients
-  double* TAU = LC + (QMAX + 1);                 // [QMAX+2] step history
-  JR* A = reinterpret_cast<JR*>(TAU + (QMAX + 2));  // [N][LDA] Jacobian, then its LU
-  JR* XS = A + N * LDA;                          // [N] solve vector
-  JR* RX = XS + N;                               // [NR][RXW] Jacobian partials
-  int* PIV = reinterpret_cast<int*>(RX + wbdf::RXW * NR);
-
-  const long long ncell = P.ncell_dev ? (long long)*P.ncell_dev : P.ncell;
-  const int qmax = max(1, min(P.max_order, QMAX));
-  const double tout = P.dt;
-
-  // ---- lane-distributed vectors: element i = lane + 32 r ----
+  constexpr int R = (N + 31) / 32;
+  constexpr int LDA = N + 1;
+  const int lane = threadIdx.x & 31;
   auto idx = [&](int r) { return lane + 32 * r; };
   auto bcast = [&](const double (&v)[R], int i) -> double {
     return __shfl_sync(0xffffffffu, v[i >> 5], i & 31);
   };
-  double ewt[R];
-  auto wms = [&](const double (&v)[R]) -> double {  // squared WRMS norm
-    double s = 0.0;
-#pragma unroll
-    for (int r = 0; r < R; ++r)
-      if (idx(r) < N) { const double x = v[r] * ewt[r]; s = fma(x, x, s); }
-    return warp_sum(s) * (1.0 / N);
-  };
-
-  // ---- right-hand side: f = [W_k wdot_k + F_k, dT/dt] at y ----
-  auto rhs = [&](const double (&y)[R], double (&f)[R]) {
-    WVec<M> yv;
-#pragma unroll
-    for (int r = 0; r < R; ++r) yv.v[r] = y[r];
-    const WVec<M> fv = warp_rhs<M>(yv, CS, GS, QS, FRC);
-#pragma unroll
-    for (int r = 0; r < R; ++r) f[r] = fv.v[r];
-  };
-
-  // ---- analytic Jacobian into A (equations of jac_table, mech_tables.cuh), in type JR ----
   auto jacobian = [&](const double (&y)[R]) {
     using namespace jac_detail;
     const JR T = (JR)bcast(y, NS);
@@ -460,6 +423,62 @@ __global__ void __launch_bounds__(WPB * 32, 1) bdf_warp_kernel(const ReactParams
     }
     return true;
   };
+  jacobian(yv.v);
+  return factor(gamma);
+}
+
+template <class M, class JR, int WPB>
+__global__ void __launch_bounds__(WPB * 32, 1) bdf_warp_kernel(const ReactParams P) {
+  using namespace bdf;
+  using Tab = typename M::TabG;
+  constexpr int N = M::N, NS = M::NS, NR = M::NR;
+  constexpr int R = (N + 31) / 32;   // vector elements per lane
+  constexpr int LDA = N + 1;         // padded matrix row
+  constexpr bool MIXED = sizeof(JR) == sizeof(float);
+  extern __shared__ __align__(16) unsigned char wsmem[];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  unsigned char* base = wsmem + (size_t)wid * bdf_warp_smem_per_warp<M, JR>();
+  double* Z = reinterpret_cast<double*>(base);   // [(QMAX+2)][N]
+  double* FRC = Z + (QMAX + 2) * N;              // [N] forcing (rhoY, then rho h)
+  double* CS = FRC + N;                          // [NS] concentrations
+  double* GS = CS + NS;                          // [NS] g/RT
+  double* QS = GS + NS;                          // [NR] rates of progress
+  double* LC = QS + NR;                          // [QMAX+1] l coefficients
+  double* TAU = LC + (QMAX + 1);                 // [QMAX+2] step history
+  JR* A = reinterpret_cast<JR*>(TAU + (QMAX + 2));  // [N][LDA] Jacobian, then its LU
+  JR* XS = A + N * LDA;                          // [N] solve vector
+  JR* RX = XS + N;                               // [NR][RXW] Jacobian partials
+  int* PIV = reinterpret_cast<int*>(RX + wbdf::RXW * NR);
+
+  const long long ncell = P.ncell_dev ? (long long)*P.ncell_dev : P.ncell;
+  const int qmax = max(1, min(P.max_order, QMAX));
+  const double tout = P.dt;
+
+  // ---- lane-distributed vectors: element i = lane + 32 r ----
+  auto idx = [&](int r) { return lane + 32 * r; };
+  auto bcast = [&](const double (&v)[R], int i) -> double {
+    return __shfl_sync(0xffffffffu, v[i >> 5], i & 31);
+  };
+  double ewt[R];
+  auto wms = [&](const double (&v)[R]) -> double {  // squared WRMS norm
+    double s = 0.0;
+#pragma unroll
+    for (int r = 0; r < R; ++r)
+      if (idx(r) < N) { const double x = v[r] * ewt[r]; s = fma(x, x, s); }
+    return warp_sum(s) * (1.0 / N);
+  };
+
+  // ---- right-hand side: f = [W_k wdot_k + F_k, dT/dt] at y ----
+  auto rhs = [&](const double (&y)[R], double (&f)[R]) {
+    WVec<M> yv;
+#pragma unroll
+    for (int r = 0; r < R; ++r) yv.v[r] = y[r];
+    const WVec<M> fv = warp_rhs<M>(yv, CS, GS, QS, FRC);
+#pragma unroll
+    for (int r = 0; r < R; ++r) f[r] = fv.v[r];
+  };
+
+  // ---- analytic Jacobian into A (equations of jac_table, mech_tables.cuh), in type JR ----
   auto solve = [&](double (&b)[R]) {
 #pragma unroll
     for (int r = 0; r < R; ++r)
@@ -695,9 +714,11 @@ __global__ void __launch_bounds__(WPB * 32, 1) bdf_warp_kernel(const ReactParams
         ++nfe;
         bool jcur = false;
         if (call_setup) {
-          jacobian(y);
+          WVec<M> yv;
+#pragma unroll
+          for (int r = 0; r < R; ++r) yv.v[r] = y[r];
           ++nje;
-          const bool ok = factor(gamma);
+          const bool ok = warp_setup<M, JR>(yv, gamma, FRC, A, XS, RX, PIV);
           gammap = gamma;
           gamrat = 1.0;
           crate2 = 1.0;
