@@ -460,7 +460,7 @@ def default_cpu_sample(cfg):
 
 
 # ---------------------------------------------------------------- CPU (oracle) legs
-def cpu_baseline(cfg, cs, sample, nthreads=0):
+def cpu_baseline(cfg, cs, sample, nthreads=0, single_core=True):
     """The oracle (C++ CVODE-class restatement, OpenMP) on a seeded uniform subsample."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
@@ -475,9 +475,18 @@ def cpu_baseline(cfg, cs, sample, nthreads=0):
     out = om.react(cs.rY[idx], cs.rYsrc[idx], cs.T[idx], cs.rE[idx], cs.rEsrc[idx], cs.mask[idx],
                    cfg.dt, cfg.rtol, cfg.atol, nthreads=cores)
     dt = time.perf_counter() - t0
-    return {"value": idx.size / dt, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"{idx.size} cells drawn uniformly (seed 99) from the same workload; "
-                      f"{dt:.2f} s wall on {cores} threads", "nfail": int(out[4])}
+    res = {"value": idx.size / dt, "unit": UNIT, "cores": cores, "kind": "port",
+           "sample": f"{idx.size} cells drawn uniformly (seed 99) from the same workload; "
+                     f"{dt:.2f} s wall on {cores} threads", "nfail": int(out[4])}
+    if single_core and cores > 1:
+        # one core on a smaller sample (about 2 s), for the per-core rate
+        n1 = max(256, min(idx.size, int(2.0 * idx.size / dt / cores)))
+        i1 = idx[:n1]
+        t0 = time.perf_counter()
+        om.react(cs.rY[i1], cs.rYsrc[i1], cs.T[i1], cs.rE[i1], cs.rEsrc[i1], cs.mask[i1], cfg.dt, cfg.rtol,
+                 cfg.atol, nthreads=1)
+        res["single_core"] = {"value": n1 / (time.perf_counter() - t0), "cells": int(n1)}
+    return res
 
 
 def run_reference(args, ws, rank, pg):
@@ -490,7 +499,7 @@ def run_reference(args, ws, rank, pg):
     sample = args.cpu_sample or default_cpu_sample(cfg) // 4
     vals = []
     for i in range(args.warmup + args.steps):
-        res = cpu_baseline(cfg, cs, sample)
+        res = cpu_baseline(cfg, cs, sample, single_core=False)
         if i >= args.warmup:
             vals.append(res)
     value = float(np.mean([v["value"] for v in vals]))

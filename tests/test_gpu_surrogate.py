@@ -30,8 +30,9 @@ ACCEPT_ALL = ("gb.sg.mis=1e30 gb.sg.cons=1e30 gb.sg.disT=1e30 gb.sg.disY=1e30 gb
 
 def _report(name, d):
     import json
-    os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
-    with open(os.path.join(ROOT, "gpurun_out", "surrogate_tests.jsonl"), "a") as f:
+    out = os.environ.get("PGB_TEST_OUT", os.path.join(ROOT, "test_reports"))
+    os.makedirs(out, exist_ok=True)
+    with open(os.path.join(out, "surrogate_tests.jsonl"), "a") as f:
         f.write(json.dumps({"test": name, **d}) + "\n")
 
 

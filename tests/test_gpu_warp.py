@@ -18,7 +18,7 @@ from helpers import boxes_from_cells, gather, tol_ratio
 from pelelm_gb300.reactor import ReactorBase
 from pelelm_gb300.workloads import CONFIGS, make_cells, mech_path
 
-OUT = os.environ.get("PGB_TEST_OUT", "gpurun_out")
+OUT = os.environ.get("PGB_TEST_OUT", "test_reports")
 
 
 def _report(name, d):
