@@ -87,3 +87,55 @@ def test_box_arena_roundtrip():
     lay = box_layout([4, 2, 3])
     a = np.random.default_rng(0).normal(size=(lay.ncell, 5))
     np.testing.assert_array_equal(from_box_arena(lay, to_box_arena(lay, a), 5), a)
+
+
+def test_global_tables_species_reaction_lists_match_stoichiometry():
+    """The warp kernel's tables: reactions grouped by kind, and per species the list of
+    (reaction, net coefficient) that turns rates of progress into production rates."""
+    import re
+    from pelelm_gb300.mech.codegen import gen_tables
+    from pelelm_gb300.workloads import load_mechanism
+    for name in ("lidryer_syn", "drm19_syn", "gri_syn"):
+        m = load_mechanism(name)
+        txt = gen_tables(m, "global")
+
+        def arr(nm):
+            body = re.search(nm + r"\[[^\]]*\] = \{([^}]*)\}", txt).group(1)
+            return [float(x.rstrip("ul")) if "." in x or "e" in x else int(x, 0) for x in body.split(",")]
+
+        off, jj, nu = arr("kSpRxOff"), arr("kSpRxJ"), arr("kSpRxNu")
+        # reaction order in the table: grouped by kind, stable within a kind
+        kinds = {"elementary": 0, "three_body": 1, "falloff": 2}
+        order = sorted(range(m.nr), key=lambda j: (kinds[m.reactions[j].kind], j))
+        S = np.zeros((m.ns, m.nr))
+        for jt, j in enumerate(order):
+            r = m.reactions[j]
+            for sp, v in r.products.items():
+                S[m.index(sp), jt] += v
+            for sp, v in r.reactants.items():
+                S[m.index(sp), jt] -= v
+        C = np.zeros_like(S)
+        for k in range(m.ns):
+            for e in range(off[k], off[k + 1]):
+                C[k, jj[e]] += nu[e]
+        assert np.array_equal(C, S), name
+        # the lists are in reaction order (the gather sums in the order the per-thread RHS does)
+        for k in range(m.ns):
+            assert jj[off[k]:off[k + 1]] == sorted(jj[off[k]:off[k + 1]])
+
+
+def test_gri_generator_species_saturated_and_recombinations_exothermic():
+    from pelelm_gb300.mech.generate import _dH298
+    from pelelm_gb300.mech.model import R_CAL
+    from pelelm_gb300.workloads import load_mechanism
+    m = load_mechanism("gri_syn")
+    for s in m.species:
+        c = s.composition
+        assert c.get("H", 0) <= 2 * c.get("C", 0) + c.get("N", 0) + 2, s.name
+    sp = {s.name: s for s in m.species}
+    for r in m.reactions:
+        if r.kind == "elementary":
+            continue
+        lhs = [n for n, v in r.reactants.items() for _ in range(v)]
+        rhs = [n for n, v in r.products.items() for _ in range(v)]
+        assert _dH298(sp, lhs, rhs) * R_CAL / 1000.0 < -20.0, r.equation()
