@@ -210,7 +210,7 @@ def run_gb(args, ws, rank, local, pg):
     work = {k: v.clone() for k, v in pristine.items()}
     work["FC"] = torch.zeros(ncell, dtype=torch.float64, device="cuda")
     views = box_views(torch, lay, work, ns)
-    base_opts = f"ode.rtol={cfg.rtol} ode.atol={cfg.atol} gb.graph=1"
+    base_opts = f"ode.rtol={cfg.rtol} ode.atol={cfg.atol} gb.graph=1 gb.autotune=1"
 
     def make_reactor(precision, extra=""):
         r = ReactorBase.create("ReactorCvode", cfg.mech, f"{base_opts} gb.precision={precision} {extra}")
@@ -250,6 +250,7 @@ def run_gb(args, ws, rank, local, pg):
     r = make_reactor(args.precision, sg_opts)
     t_step, clocks, st = timed_steps(r, args.steps, args.warmup)
     sst = r.surrogate_stats() if surrogate else None
+    tuning = r.tuning()
     t_max = allmax(pg, t_step)
     value = allsum(pg, float(ncell * args.steps)) / t_max
     ms_per_step = 1e3 * t_max / args.steps
@@ -360,7 +361,8 @@ def run_gb(args, ws, rank, local, pg):
                              "state restored between steps",
                        "launch": "surrogate kernel -> persistent work-stealing BDF on the device fallback "
                                  "list -> audit kernel, one CUDA graph per step" if surrogate else
-                                 "one persistent work-stealing kernel per step, CUDA-graph replay"},
+                                 "one persistent work-stealing kernel per step, CUDA-graph replay",
+                       "autotune": tuning},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
                          "frac": achieved / fp64_peak,

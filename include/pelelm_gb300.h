@@ -63,7 +63,9 @@ typedef struct {
  * options: whitespace/semicolon separated key=value pairs — the reference's runtime keys
  * ode.rtol, ode.atol, cvode.max_order, cvode.solve_type, ode.analytical_jacobian,
  * peleLM.use_typ_vals_chem, plus ode.max_steps, gb.precision=fp64|mixed, gb.tpb, gb.graph=0|1,
- * gb.history=shared|global, gb.lu=shared|global, and gb.surrogate=<file> (learned surrogate
+ * gb.history=shared|global, gb.lu=shared|global, gb.mapping=thread|warp, gb.wpb, gb.autotune=0|1
+ * (time every compiled mapping on the first advance's cells, keep the fastest), and
+ * gb.surrogate=<file> (learned surrogate
  * with BDF fallback; no reference counterpart) with threshold overrides gb.sg.audit (audit
  * fraction), gb.sg.mis [K], gb.sg.cons, gb.sg.disT [K], gb.sg.disY, gb.sg.neg,
  * gb.sg.ood_margin, gb.sg.tol_T, gb.sg.tol_Y, gb.sg.models, gb.sg.seed.
@@ -103,6 +105,11 @@ typedef struct pgb_chem_view {
   pgb_array4 rhoY, rhoY_src, T, rhoH, rhoH_src, FC, mask, I_R;
 } pgb_chem_view;
 int pgb_advance_chemistry(pgb_reactor* r, const pgb_chem_view* views, int nbox, double dt, void* stream);
+
+/* Report of the autotuner (reactor created with gb.autotune=1): the time of one advance of a
+ * sample of the first call's cells with every compiled BDF mapping and the one kept; empty
+ * before the first advance. Returns the report's length. No counterpart in the reference. */
+int pgb_reactor_tuning(pgb_reactor* r, char* buf, size_t n);
 
 /* Waits for the last advance on its stream and returns its counters. */
 int pgb_reactor_get_stats(pgb_reactor* r, pgb_stats* out);

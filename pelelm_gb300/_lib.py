@@ -61,6 +61,7 @@ EXPORTS = {
     "pgb_reactor_surrogate_raw": (C.c_int, [_vp, _vp, C.c_int, _vp, _vp, _vp]),
     "pgb_heat_release": (C.c_int, [C.c_char_p, _vp, _vp, _vp, _vp, _vp]),
     "pgb_advance_chemistry": (C.c_int, [_vp, _vp, C.c_int, C.c_double, _vp]),
+    "pgb_reactor_tuning": (C.c_int, [_vp, C.c_char_p, C.c_size_t]),
     "pgb_reactor_close": (None, [_vp]),
     "pgb_reaction_rates": (C.c_int, [C.c_char_p, C.POINTER(BoxView), C.POINTER(Array4), _vp]),
     "pgb_rhoh_to_temp": (C.c_int, [C.c_char_p, C.POINTER(BoxView), C.c_double, C.c_double, _vp]),

@@ -60,6 +60,7 @@ struct Options {
   int lu_global = -1;      // gb.lu = shared | global (L2-resident Jacobian/LU); -1 = auto
   int mapping = -1;        // gb.mapping = thread (cell per thread) | warp (cell per warp); -1 = auto
   int wpb = 0;             // gb.wpb: warps per block of the warp mapping (0 = most that fit)
+  bool autotune = false;   // gb.autotune: time the compiled mappings on the first advance's cells
   std::string solve_type = "denseAJ_direct";
   int analytical_jacobian = 1;
   std::string surrogate;   // gb.surrogate = trained surrogate file: surrogate + BDF fallback
@@ -97,6 +98,7 @@ int parse_options(const char* s, Options& o) {
         else if (v == "warp") o.mapping = 1;
         else return set_err("gb.mapping must be thread or warp, got '%s'", v.c_str());
       } else if (k == "gb.wpb") o.wpb = std::stoi(v);
+      else if (k == "gb.autotune") o.autotune = std::stoi(v) != 0;
       else if (k == "gb.surrogate") o.surrogate = v;
       else if (k == "gb.sg.audit") o.sg.audit_frac = std::stod(v);
       else if (k == "gb.sg.mis") o.sg.mis = std::stod(v);
@@ -210,6 +212,8 @@ struct pgb_reactor {
   cudaStream_t last_stream = nullptr;
   int device = 0, nsm = 0;
   SgModel sg;  // loaded when options name a surrogate file
+  bool tuned = false;
+  std::string tuning;  // autotuner report
 };
 
 namespace {
@@ -500,9 +504,152 @@ namespace {
 
 // Enqueues one advance of the prepared box table on `st` (a captured graph is replayed when the
 // box table and dt repeat); the caller holds r->mu.
+}  // namespace
+
+namespace pgb_tune {
+
+// Copies cells c = i * stride (i < nsample) of the box table into a single-box arena, one
+// component-major block per field: rhoY (ns), rhoY forcing (ns), T, rho h, rho h forcing, FC.
+__global__ void gather_sample_kernel(const pgb::BoxDev* boxes, int nbox, int ns, long long nsample, long long stride,
+                                     double* arena) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nsample; i += (long long)gridDim.x * blockDim.x) {
+    const long long c = i * stride;
+    int lo = 0, hi = nbox - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (boxes[mid].cell_offset <= c) lo = mid; else hi = mid - 1;
+    }
+    const pgb::BoxDev& B = boxes[lo];
+    long long r = c - B.cell_offset;
+    const int ci = B.lo0 + (int)(r % B.len0);
+    r /= B.len0;
+    const int cj = B.lo1 + (int)(r % B.len1);
+    const int ck = B.lo2 + (int)(r / B.len1);
+    auto at = [&](const pgb::ArrDev& a, int n) {
+      return a.p[(long long)(ci - a.begin0) + (long long)(cj - a.begin1) * a.jstride + (long long)(ck - a.begin2) * a.kstride +
+                 (long long)n * a.nstride];
+    };
+    for (int k = 0; k < ns; ++k) {
+      arena[(size_t)k * nsample + i] = at(B.rY, k) * B.sY_in;
+      arena[(size_t)(ns + k) * nsample + i] = at(B.rYsrc, k) * B.sY_in;
+    }
+    arena[(size_t)(2 * ns) * nsample + i] = at(B.T, 0);
+    arena[(size_t)(2 * ns + 1) * nsample + i] = at(B.rE, 0) * B.sE_in;
+    arena[(size_t)(2 * ns + 2) * nsample + i] = at(B.rEsrc, 0) * B.sE_in;
+    arena[(size_t)(2 * ns + 3) * nsample + i] = 0.0;
+  }
+}
+
+}  // namespace pgb_tune
+
+namespace {
+
+// gb.autotune: on the first advance, copy a strided sample of the caller's cells (at most
+// 32768) into reactor scratch and time one advance of it with every compiled BDF mapping
+// (cell per thread with the planner's layout; cell per warp at each compiled warps-per-block
+// size whose shared memory fits); keep the fastest for the life of the reactor. The caller's
+// arrays are only read. The surrogate (if any) is not part of the timing.
+int run_autotune(pgb_reactor* r, const std::vector<pgb::BoxDev>& boxes, long long ncell, double dt, cudaStream_t st) {
+  r->tuned = true;
+  const MechEntry& m = *r->mech;
+  const int ns = m.ns, nf = 2 * ns + 4;
+  const long long nsample = std::min<long long>(ncell, 32768);
+  const long long stride = std::max<long long>(1, ncell / nsample);
+  const size_t arena_bytes = (size_t)nf * nsample * sizeof(double);
+  struct Cand { int mapping, wpb; };
+  std::vector<Cand> cands;
+  if (m.bdf_mixed) cands.push_back({0, 0});
+  const int per = r->opt.mixed ? m.wsmem_mixed : m.wsmem_fp64;
+  for (int i = 0; i < 4 && m.wpb_choice[i] > 0; ++i)
+    if (m.wpb_choice[i] * per <= kMaxSmemPerBlock) cands.push_back({1, m.wpb_choice[i]});
+  if (cands.size() < 2) {
+    r->tuning = "single compiled mapping: nothing to tune";
+    return 0;
+  }
+  double* pristine = nullptr;
+  double* work = nullptr;
+  pgb::BoxDev* d_src = nullptr;
+  Scratch sc;
+  int rc = 0;
+  const Options saved = r->opt;
+  SgModel sg_saved = r->sg;
+  r->sg.d_net = nullptr;  // time the BDF alone
+  auto fail = [&](const char* what) { rc = set_err("autotune: %s", what); };
+  do {
+    if (cudaMalloc(&pristine, arena_bytes) != cudaSuccess || cudaMalloc(&work, arena_bytes) != cudaSuccess ||
+        cudaMalloc(&d_src, boxes.size() * sizeof(pgb::BoxDev)) != cudaSuccess) { fail("out of memory"); break; }
+    if (cudaMemcpyAsync(d_src, boxes.data(), boxes.size() * sizeof(pgb::BoxDev), cudaMemcpyHostToDevice, st) != cudaSuccess) {
+      fail("box copy"); break;
+    }
+    pgb_tune::gather_sample_kernel<<<(int)std::min<long long>((nsample + 255) / 256, 1024), 256, 0, st>>>(
+        d_src, (int)boxes.size(), ns, nsample, stride, pristine);
+    if (cudaGetLastError() != cudaSuccess) { fail("gather launch"); break; }
+    if (cudaMalloc(&sc.d_counter, sizeof(unsigned long long)) != cudaSuccess ||
+        cudaMalloc(&sc.d_stats, sizeof(pgb::ReactStats)) != cudaSuccess ||
+        cudaMalloc(&sc.d_boxes, sizeof(pgb::BoxDev)) != cudaSuccess ||
+        cudaMallocHost(&sc.h_boxes, sizeof(pgb::BoxDev)) != cudaSuccess) { fail("out of memory"); break; }
+    sc.box_cap = 1;
+    pgb::BoxDev& b = *sc.h_boxes;
+    std::memset(&b, 0, sizeof(b));
+    b.len0 = (int)nsample; b.len1 = 1; b.len2 = 1;
+    b.sY_in = b.sE_in = b.sY_out = b.sE_out = 1.0;
+    auto field = [&](int f) {
+      pgb::ArrDev a;
+      std::memset(&a, 0, sizeof(a));
+      a.p = work + (size_t)f * nsample;
+      a.jstride = nsample; a.kstride = nsample; a.nstride = nsample;
+      return a;
+    };
+    b.rY = field(0); b.rYsrc = field(ns); b.T = field(2 * ns); b.rE = field(2 * ns + 1); b.rEsrc = field(2 * ns + 2);
+    b.FC = field(2 * ns + 3);
+    cudaEvent_t e0, e1;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) { fail("events"); break; }
+    std::ostringstream rep;
+    double best = 1e300;
+    Cand pick = cands[0];
+    for (const Cand& c : cands) {
+      r->opt.mapping = c.mapping;
+      r->opt.wpb = c.wpb;
+      const LaunchPlan pl = plan_launch(r, nsample);
+      if (ensure_buf(sc, sc.d_z, sc.z_cap, pl.z_bytes) || ensure_buf(sc, sc.d_lu, sc.lu_cap, pl.lu_bytes)) { rc = -1; break; }
+      float ms = 0.f;
+      for (int rep_i = 0; rep_i < 2 && !rc; ++rep_i) {  // warm-up launch, then the timed one
+        if (cudaMemcpyAsync(work, pristine, arena_bytes, cudaMemcpyDeviceToDevice, st) != cudaSuccess) { fail("copy"); break; }
+        cudaEventRecord(e0, st);
+        if (enqueue_advance(r, sc, 1, nsample, dt, st)) { rc = -1; break; }
+        cudaEventRecord(e1, st);
+        if (cudaEventSynchronize(e1) != cudaSuccess) { fail("timed advance failed"); break; }
+        cudaEventElapsedTime(&ms, e0, e1);
+      }
+      if (rc) break;
+      rep << (c.mapping ? "warp/" : "thread") << (c.mapping ? std::to_string(c.wpb) : std::string()) << " " << ms
+          << " ms; ";
+      if (ms < best) { best = ms; pick = c; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) break;
+    r->opt = saved;
+    r->opt.mapping = pick.mapping;
+    r->opt.wpb = pick.wpb;
+    rep << "on " << nsample << " sample cells -> " << (pick.mapping ? "warp/" + std::to_string(pick.wpb) : std::string("thread"));
+    r->tuning = rep.str();
+  } while (false);
+  if (rc) r->opt = saved;
+  r->sg = sg_saved;
+  cudaStreamSynchronize(st);
+  if (pristine) cudaFree(pristine);
+  if (work) cudaFree(work);
+  if (d_src) cudaFree(d_src);
+  free_scratch(sc);
+  return rc;
+}
+
 int advance_box_table(pgb_reactor* r, const std::vector<pgb::BoxDev>& boxes, long long ncell, double dt_react,
                       cudaStream_t st) {
   const int nbox = (int)boxes.size();
+  if (r->opt.autotune && !r->tuned && !r->null_reactor && ncell > 0 && run_autotune(r, boxes, ncell, dt_react, st))
+    return -1;
   Scratch* s = nullptr;
   if (ensure_scratch(r, st, std::max(nbox, 1), &s)) return -1;
   if (!r->null_reactor) {
@@ -587,6 +734,16 @@ int pgb_advance_chemistry(pgb_reactor* r, const pgb_chem_view* views, int nbox, 
     if (views[b].I_R.p) boxes[b].IR = arr_dev(views[b].I_R);
   }
   return advance_box_table(r, boxes, ncell, dt, static_cast<cudaStream_t>(stream));
+}
+
+int pgb_reactor_tuning(pgb_reactor* r, char* buf, size_t n) {
+  if (!r) return set_err("null reactor");
+  std::lock_guard<std::mutex> g(r->mu);
+  if (buf && n) {
+    std::strncpy(buf, r->tuning.c_str(), n - 1);
+    buf[n - 1] = 0;
+  }
+  return (int)r->tuning.size();
 }
 
 int pgb_reactor_get_stats(pgb_reactor* r, pgb_stats* out) {

@@ -122,6 +122,12 @@ class ReactorGB:
         return {"ncell": s.ncell, "nst": s.nst, "nfe": s.nfe, "nje": s.nje, "netf": s.netf,
                 "ncfn": s.ncfn, "nfail": s.nfail, "max_nst": s.max_nst, "hist": list(s.hist)}
 
+    def tuning(self) -> str:
+        """The autotuner's report (gb.autotune=1), empty before the first advance."""
+        buf = C.create_string_buffer(4096)
+        check(min(0, lib().pgb_reactor_tuning(self._h, buf, 4096)), "tuning")
+        return buf.value.decode()
+
     def surrogate_stats(self) -> dict:
         """Counters of the learned surrogate in the last advance (reactor made with gb.surrogate)."""
         s = _lib.SurrogateStats()

@@ -145,3 +145,28 @@ def test_gri_thread_mapping_and_pointwise_rates_are_refused(native_lib, cuda):
         ReactorBase.create("ReactorCvode", "gri_syn", "gb.mapping=thread").init(2, 1)
     with pytest.raises(RuntimeError, match="surrogate"):
         ReactorBase.create("ReactorCvode", "gri_syn", "gb.surrogate=x.pgbs").init(2, 1)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("cfgname", ["drm19_2M", "lidryer_amr120"])
+def test_autotuner_picks_a_compiled_mapping_and_leaves_inputs_alone(native_lib, cuda, cfgname):
+    """gb.autotune=1 times every compiled mapping on a sample of the first call's cells and
+    keeps the fastest; the advance then equals, bit for bit, one made with that mapping given
+    explicitly (so the tuning only read the caller's arrays)."""
+    torch = cuda
+    cfg = CONFIGS[cfgname]
+    cs = make_cells(cfg, 4 * 16 ** 3, seed=8)
+    (a, _) = _run(torch, cfg, cs, [16] * 4, "gb.precision=mixed gb.autotune=1")
+    r = ReactorBase.create("ReactorCvode", cfg.mech, f"ode.rtol={cfg.rtol} ode.atol={cfg.atol} gb.autotune=1")
+    r.init(2, 1)
+    r.react_boxes(boxes_from_cells(torch, cs, [16] * 4), cfg.dt, 0.0)
+    torch.cuda.synchronize()
+    rep = r.tuning()
+    r.close()
+    _report(f"autotune[{cfgname}]", {"report": rep})
+    assert "->" in rep and "thread" in rep and "warp/" in rep
+    picked = rep.split("->")[-1].strip()
+    explicit = "gb.mapping=thread" if picked == "thread" else f"gb.mapping=warp gb.wpb={picked.split('/')[1]}"
+    (b, _) = _run(torch, cfg, cs, [16] * 4, "gb.precision=mixed " + explicit)
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
