@@ -297,31 +297,37 @@ __device__ __noinline__ bool warp_setup(const WVec<M> yv, const double gamma, co
     Qw = warp_sum(Qw);
     cpw = warp_sum(cpw);
     __syncwarp();
-    // (2) assembly in reaction order; lane owns columns k = lane + 32 c (k == NS: T column)
-#pragma unroll 1
-    for (int j = 0; j < NR; ++j) {
-      const TabReaction<JR>& r = Tab::template rx<JR>(j);
-      const JR* pj = RX + j * wbdf::RXW;
-#pragma unroll 1
-      for (int row = 0; row < r.nr + r.np; ++row) {
-        const bool isr = row < r.nr;
-        const int i = isr ? r.rs[row] : r.ps[row - r.nr];
-        const JR sgnW = (isr ? JR(-1) : JR(1)) * Tab::template sp<JR>(i).W;
+    // (2) assembly: lane owns species k = lane + 32 c and walks, in reaction order, only the
+    // reactions whose terms land in column k (k reacts, or a third body) — adding into column k
+    // and, where k is a slot species, into row k of the T column. Every matrix entry receives
+    // its additions in reaction order, then slot order, whatever the lane schedule.
 #pragma unroll
-        for (int cc = 0; cc < R; ++cc) {
-          const int k = idx(cc);
-          if (k > NS) continue;
-          if (k == NS) { A[i * LDA + NS] += sgnW * pj[0]; continue; }
-          JR v = JR(0);
-          for (int s = 0; s < r.nr; ++s) if (r.rs[s] == k) v += pj[1 + s];
-          for (int s = 0; s < r.np; ++s) if (r.ps[s] == k) v += pj[4 + s];
-          if (r.kind != 0) {
-            JR eff = JR(1);
-            const TabThirdBody<JR>& t = Tab::template tb<JR>(r.tb);
-            for (int e = 0; e < t.n; ++e) if (t.sp[e] == k) eff += t.effm1[e];
-            v += pj[7] * eff;
-          }
-          if (v != JR(0)) A[i * LDA + k] += sgnW * Tab::template sp<JR>(k).invW * v;
+    for (int cc = 0; cc < R; ++cc) {
+      const int k = idx(cc);
+      if (k >= NS) continue;
+      const JR iwk = Tab::template sp<JR>(k).invW;
+      const int e1 = Tab::col_end(k);
+#pragma unroll 1
+      for (int e = Tab::col_begin(k); e < e1; ++e) {
+        const int j = Tab::col_j(e);
+        const TabReaction<JR>& r = Tab::template rx<JR>(j);
+        const JR* pj = RX + j * wbdf::RXW;
+        JR v = JR(0);
+        for (int s = 0; s < r.nr; ++s) if (r.rs[s] == k) v += pj[1 + s];
+        for (int s = 0; s < r.np; ++s) if (r.ps[s] == k) v += pj[4 + s];
+        if (r.kind != 0) {
+          JR eff = JR(1);
+          const TabThirdBody<JR>& t = Tab::template tb<JR>(r.tb);
+          for (int q = 0; q < t.n; ++q) if (t.sp[q] == k) eff += t.effm1[q];
+          v += pj[7] * eff;
+        }
+#pragma unroll 1
+        for (int row = 0; row < r.nr + r.np; ++row) {
+          const bool isr = row < r.nr;
+          const int i = isr ? r.rs[row] : r.ps[row - r.nr];
+          const JR sgnW = (isr ? JR(-1) : JR(1)) * Tab::template sp<JR>(i).W;
+          if (i == k) A[k * LDA + NS] += sgnW * pj[0];
+          if (v != JR(0)) A[i * LDA + k] += sgnW * iwk * v;
         }
       }
     }

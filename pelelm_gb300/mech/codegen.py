@@ -559,6 +559,17 @@ def gen_tables(m: Mechanism, space: str = "constant") -> str:
                     jj.append(j)
                     nu.append(float(net))
             off.append(len(jj))
+        # per species: the reactions whose Jacobian terms land in its column (it is a reactant or
+        # product, or the reaction has a third body: every species is a collider), in order
+        coff, cj = [0], []
+        for k in range(ns):
+            for j, (_, _, _, kind_, _, rs_, ps_, _, _, _) in enumerate(rx):
+                if k in rs_ or k in ps_ or kind_ != 0:
+                    cj.append(j)
+            coff.append(len(cj))
+        e(f"constexpr int NCOL = {len(cj)};")
+        e(f"{qual} int kColOff[NS + 1] = {{{', '.join(str(x) for x in coff)}}};")
+        e(f"{qual} int kColJ[NCOL] = {{{', '.join(str(x) for x in cj)}}};")
         e(f"constexpr int NSPRX = {len(jj)};")
         e(f"{qual} int kSpRxOff[NS + 1] = {{{', '.join(str(x) for x in off)}}};")
         e(f"{qual} int kSpRxJ[NSPRX] = {{{', '.join(str(x) for x in jj)}}};")
@@ -570,6 +581,9 @@ def gen_tables(m: Mechanism, space: str = "constant") -> str:
         e("  __device__ static int sprx_end(int k) { return kSpRxOff[k + 1]; }")
         e("  __device__ static int sprx_j(int e) { return kSpRxJ[e]; }")
         e("  __device__ static double sprx_nu(int e) { return kSpRxNu[e]; }")
+        e("  __device__ static int col_begin(int k) { return kColOff[k]; }")
+        e("  __device__ static int col_end(int k) { return kColOff[k + 1]; }")
+        e("  __device__ static int col_j(int e) { return kColJ[e]; }")
     for nm, typ, arr in (("sp", "TabSpecies", "kSpecies"), ("rx", "TabReaction", "kReactions"),
                          ("tb", "TabThirdBody", "kThirdBody"), ("troe", "TabTroe", "kTroe")):
         e(f"  template <class R> __device__ static const {typ}<R>& {nm}(int i) {{")
