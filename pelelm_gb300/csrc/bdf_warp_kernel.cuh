@@ -39,7 +39,7 @@ template <class M, class JR>
 __host__ __device__ constexpr int bdf_warp_smem_per_warp() {
   constexpr int N = M::N, NS = M::NS, NR = M::NR;
   constexpr int nd = (QMAX + 2) * N + N + 2 * NS + NR + (QMAX + 1) + (QMAX + 2);
-  constexpr int nj = N * (N + 1) + N + wbdf::RXW * NR;
+  constexpr int nj = N * (N + 1) + N + wbdf::RXW * NR + 4 * NS;
   return ((nd * 8 + nj * (int)sizeof(JR) + N * 4) + 15) / 16 * 16;
 }
 
@@ -181,7 +181,7 @@ __device__ __noinline__ WVec<M> warp_rhs(const WVec<M> yv, double* CS, double* G
 // it would otherwise share the instruction cache with the step loop). False: singular.
 template <class M, class JR>
 __device__ __noinline__ bool warp_setup(const WVec<M> yv, const double gamma, const double* FRC, JR* A,
-                                        JR* XS, JR* RX, int* PIV) {
+                                        JR* XS, JR* RX, JR* TH, int* PIV) {
   using Tab = typename M::TabG;
   constexpr int N = M::N, NS = M::NS, NR = M::NR;
   constexpr int R = (N + 31) / 32;
@@ -199,14 +199,26 @@ __device__ __noinline__ bool warp_setup(const WVec<M> yv, const double gamma, co
     const JR lnT1 = JR(1) - lnT;
     const JR lnP0RT = JR(kLnP0OverR) - lnT;
     const JR RT = JR(kRerg) * T;
+    // per species, once: concentration (the solve vector is free during the setup) and the
+    // NASA-7 terms g/RT, h/RT, cp/R, d(cp/R)/dT that the reaction and energy terms reuse
+    JR* TG = TH;
+    JR* TH_ = TH + NS;
+    JR* TC = TH + 2 * NS;
+    JR* TD = TH + 3 * NS;
     JR c_loc = JR(0);
 #pragma unroll
     for (int r = 0; r < R; ++r) {
       const int k = idx(r);
       if (k < NS) {
         const JR c = (JR)y[r] * Tab::template sp<JR>(k).invW;
-        XS[k] = c;  // the solve vector holds the concentrations during the setup
+        XS[k] = c;
         c_loc += c;
+        JR g, h, cp, d;
+        nasa<JR>(Tab::template sp<JR>(k), T, invT, lnT1, g, h, cp, d);
+        TG[k] = g;
+        TH_[k] = h;
+        TC[k] = cp;
+        TD[k] = d;
       }
     }
     const JR Ctot = warp_sum(c_loc);
@@ -259,16 +271,12 @@ __device__ __noinline__ bool warp_setup(const WVec<M> yv, const double gamma, co
       if (r.rev) {
         JR dG = -(JR)r.dnu * lnP0RT, dH = JR(0);
         for (int s = 0; s < r.np; ++s) {
-          JR g, h, c, d;
-          nasa<JR>(Tab::template sp<JR>(r.ps[s]), T, invT, lnT1, g, h, c, d);
-          dG += g;
-          dH += h;
+          dG += TG[r.ps[s]];
+          dH += TH_[r.ps[s]];
         }
         for (int s = 0; s < r.nr; ++s) {
-          JR g, h, c, d;
-          nasa<JR>(Tab::template sp<JR>(r.rs[s]), T, invT, lnT1, g, h, c, d);
-          dG -= g;
-          dH -= h;
+          dG -= TG[r.rs[s]];
+          dH -= TH_[r.rs[s]];
         }
         kr = kf * pgb_expT<JR>(fmin(dG, JR(700)));
         dlnkr = dlnkf - (dH - (JR)r.dnu) * invT;
@@ -288,10 +296,8 @@ __device__ __noinline__ bool warp_setup(const WVec<M> yv, const double gamma, co
       for (int row = 0; row < r.nr + r.np; ++row) {
         const bool isr = row < r.nr;
         const int i = isr ? r.rs[row] : r.ps[row - r.nr];
-        JR g, h, c, d;
-        nasa<JR>(Tab::template sp<JR>(i), T, invT, lnT1, g, h, c, d);
-        Qw += (isr ? -q : q) * h * RT;
-        cpw += (isr ? -q : q) * c * JR(kRerg);
+        Qw += (isr ? -q : q) * TH_[i] * RT;
+        cpw += (isr ? -q : q) * TC[i] * JR(kRerg);
       }
     }
     Qw = warp_sum(Qw);
@@ -338,8 +344,7 @@ __device__ __noinline__ bool warp_setup(const WVec<M> yv, const double gamma, co
     for (int r = 0; r < R; ++r) {
       const int k = idx(r);
       if (k < NS) {
-        JR g, h, c, d;
-        nasa<JR>(Tab::template sp<JR>(k), T, invT, lnT1, g, h, c, d);
+        const JR h = TH_[k], c = TC[k], d = TD[k];
         const JR iw = Tab::template sp<JR>(k).invW;
         const JR cpm = c * JR(kRerg) * iw, hm = h * RT * iw;
         const JR yk = (JR)y[r];
@@ -361,15 +366,9 @@ __device__ __noinline__ bool warp_setup(const WVec<M> yv, const double gamma, co
       const int k = idx(cc);
       if (k > NS) continue;
       JR acc = JR(0);
-      for (int i = 0; i < NS; ++i) {
-        JR g, h, c, d;
-        nasa<JR>(Tab::template sp<JR>(i), T, invT, lnT1, g, h, c, d);
-        acc += h * RT * Tab::template sp<JR>(i).invW * A[i * LDA + k];
-      }
+      for (int i = 0; i < NS; ++i) acc += TH_[i] * RT * Tab::template sp<JR>(i).invW * A[i * LDA + k];
       if (k < NS) {
-        JR g, h, c, d;
-        nasa<JR>(Tab::template sp<JR>(k), T, invT, lnT1, g, h, c, d);
-        A[NS * LDA + k] = -acc * invD - QD2 * c * JR(kRerg) * Tab::template sp<JR>(k).invW;
+        A[NS * LDA + k] = -acc * invD - QD2 * TC[k] * JR(kRerg) * Tab::template sp<JR>(k).invW;
       } else {
         A[NS * LDA + NS] = -(acc + cpwm) * invD - QD2 * dD;
       }
@@ -454,7 +453,8 @@ __global__ void __launch_bounds__(WPB * 32, 1) bdf_warp_kernel(const ReactParams
   JR* A = reinterpret_cast<JR*>(TAU + (QMAX + 2));  // [N][LDA] Jacobian, then its LU
   JR* XS = A + N * LDA;                          // [N] solve vector
   JR* RX = XS + N;                               // [NR][RXW] Jacobian partials
-  int* PIV = reinterpret_cast<int*>(RX + wbdf::RXW * NR);
+  JR* TH = RX + wbdf::RXW * NR;                  // [4][NS] NASA-7 terms of the setup
+  int* PIV = reinterpret_cast<int*>(TH + 4 * NS);
 
   const long long ncell = P.ncell_dev ? (long long)*P.ncell_dev : P.ncell;
   const int qmax = max(1, min(P.max_order, QMAX));
@@ -724,7 +724,7 @@ __global__ void __launch_bounds__(WPB * 32, 1) bdf_warp_kernel(const ReactParams
 #pragma unroll
           for (int r = 0; r < R; ++r) yv.v[r] = y[r];
           ++nje;
-          const bool ok = warp_setup<M, JR>(yv, gamma, FRC, A, XS, RX, PIV);
+          const bool ok = warp_setup<M, JR>(yv, gamma, FRC, A, XS, RX, TH, PIV);
           gammap = gamma;
           gamrat = 1.0;
           crate2 = 1.0;
