@@ -375,7 +375,7 @@ def run_gb(args, ws, rank, local, pg):
                                  f"x {nfe} RHS evaluations per step / BDF kernel time",
                          "peak_source": "measured in this run: pgb_fp64_peak_tflops (DFMA, full grid)"},
             "stats": {"nst_per_cell": st["nst"] / ncell, "nfe_per_cell": st["nfe"] / ncell,
-                      "nje_per_cell": st["nje"] / ncell, "max_steps_cell": st["max_nst"], "nfail": int(st["nfail"]),
+                      "nje_per_cell": st["nje"] / ncell, "max_steps_cell": st["max_nst"], "nfail": int(st["nfail"]), "nretry": int(st["nretry"]),
                       "steps_hist_log2": hist},
             "clocks": clocks,
             "gpu_launches": args.steps * (3 if surrogate else 1),

@@ -50,10 +50,12 @@ typedef struct {
 } pgb_box_view;
 
 /* Counters of the last advance (pgb_reactor_get_stats). hist[b] counts cells whose BDF step
- * count lies in [2^b, 2^(b+1)). */
+ * count lies in [2^b, 2^(b+1)). nretry counts the cells the mixed-precision pass failed and
+ * handed to the FP64 retry pass (gb.retry); nfail counts the cells that failed for good. */
 typedef struct {
   unsigned long long ncell, nst, nfe, nje, netf, ncfn, nfail, max_nst;
   unsigned long long hist[16];
+  unsigned long long nretry;
 } pgb_stats;
 
 /* ReactorBase::create(name) followed by init(reactor_type, ncells)
@@ -64,7 +66,9 @@ typedef struct {
  * ode.rtol, ode.atol, cvode.max_order, cvode.solve_type, ode.analytical_jacobian,
  * peleLM.use_typ_vals_chem, plus ode.max_steps, gb.precision=fp64|mixed, gb.tpb, gb.graph=0|1,
  * gb.history=shared|global, gb.lu=shared|global, gb.mapping=thread|warp, gb.wpb, gb.autotune=0|1
- * (time every compiled mapping on the first advance's cells, keep the fastest), and
+ * (time every compiled mapping on the first advance's cells, keep the fastest), gb.retry=0|1
+ * (default 1: cells the mixed-precision pass fails are integrated again from their inputs by
+ * the FP64 kernel in the same call), and
  * gb.surrogate=<file> (learned surrogate
  * with BDF fallback; no reference counterpart) with threshold overrides gb.sg.audit (audit
  * fraction), gb.sg.mis [K], gb.sg.cons, gb.sg.disT [K], gb.sg.disY, gb.sg.neg,

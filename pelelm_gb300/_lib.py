@@ -36,7 +36,8 @@ class ChemView(C.Structure):
 class Stats(C.Structure):
     _fields_ = [("ncell", C.c_ulonglong), ("nst", C.c_ulonglong), ("nfe", C.c_ulonglong),
                 ("nje", C.c_ulonglong), ("netf", C.c_ulonglong), ("ncfn", C.c_ulonglong),
-                ("nfail", C.c_ulonglong), ("max_nst", C.c_ulonglong), ("hist", C.c_ulonglong * 16)]
+                ("nfail", C.c_ulonglong), ("max_nst", C.c_ulonglong), ("hist", C.c_ulonglong * 16),
+                ("nretry", C.c_ulonglong)]
 
 
 class SurrogateStats(C.Structure):

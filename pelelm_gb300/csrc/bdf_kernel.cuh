@@ -336,6 +336,18 @@ __global__ void __launch_bounds__(TPB, 1) bdf_reactor_kernel(const ReactParams P
   };
   auto finish_cell = [&]() {
     const BoxDev& B = P.boxes[box];
+    if (status != OK && P.retry_list) {  // hand the cell to the retry pass, arrays untouched
+      P.retry_list[atomicAdd(P.retry_count, 1ull)] = cell;
+      ReactStats* S = P.stats;
+      atomicAdd(&S->nst, (unsigned long long)nst);
+      atomicAdd(&S->nfe, (unsigned long long)nfe);
+      atomicAdd(&S->nje, (unsigned long long)nje);
+      atomicAdd(&S->netf, (unsigned long long)netf);
+      atomicAdd(&S->ncfn, (unsigned long long)ncfn);
+      atomicAdd(&S->nretry, 1ull);
+      phase = NEED;
+      return;
+    }
     // rho h(t) = rho h0 + F_h t ; T from (h, Y) by Newton with the integrated T as guess
     const double rE = fma(tout, FRC(NS), rE0);
     double rho = 0.0;

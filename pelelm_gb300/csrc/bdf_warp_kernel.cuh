@@ -951,6 +951,20 @@ __global__ void __launch_bounds__(WPB * 32, 1) bdf_warp_kernel(const ReactParams
 
     // ---------------------------------------------- finish: rho h(t), T from (h, Y)
     __syncwarp();
+    if (status != OK && P.retry_list) {  // hand the cell to the retry pass, arrays untouched
+      if (lane == 0) {
+        P.retry_list[atomicAdd(P.retry_count, 1ull)] = cell;
+        ReactStats* S = P.stats;
+        atomicAdd(&S->nst, (unsigned long long)nst);
+        atomicAdd(&S->nfe, (unsigned long long)nfe);
+        atomicAdd(&S->nje, (unsigned long long)nje);
+        atomicAdd(&S->netf, (unsigned long long)netf);
+        atomicAdd(&S->ncfn, (unsigned long long)ncfn);
+        atomicAdd(&S->nretry, 1ull);
+      }
+      __syncwarp();
+      continue;
+    }
     const double rE = fma(tout, FRC[NS], rE0);
     double rho_l = 0.0;
 #pragma unroll

@@ -104,6 +104,8 @@ extern "C" int pgb_react_boxes_noalloc(const char* mechanism, const pgb_box_view
   p.z_scratch = nullptr;
   p.cell_list = nullptr;
   p.ncell_dev = nullptr;
+  p.retry_list = nullptr;  // a failed cell keeps its state at failure and FC = -status
+  p.retry_count = nullptr;
   int dev = 0, nsm = 0;
   PGB_CUDA(cudaGetDevice(&dev));
   PGB_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
@@ -123,6 +125,7 @@ extern "C" int pgb_react_boxes_noalloc(const char* mechanism, const pgb_box_view
     stats->nst = h.nst; stats->nfe = h.nfe; stats->nje = h.nje; stats->netf = h.netf;
     stats->ncfn = h.ncfn; stats->nfail = h.nfail; stats->max_nst = h.max_nst;
     for (int i = 0; i < 16; ++i) stats->hist[i] = h.hist[i];
+    stats->nretry = h.nretry;
   }
   return 0;
 }

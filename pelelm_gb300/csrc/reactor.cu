@@ -61,6 +61,7 @@ struct Options {
   int mapping = -1;        // gb.mapping = thread (cell per thread) | warp (cell per warp); -1 = auto
   int wpb = 0;             // gb.wpb: warps per block of the warp mapping (0 = most that fit)
   bool autotune = false;   // gb.autotune: time the compiled mappings on the first advance's cells
+  bool retry = true;       // gb.retry: cells the mixed-precision pass fails are integrated again in FP64
   std::string solve_type = "denseAJ_direct";
   int analytical_jacobian = 1;
   std::string surrogate;   // gb.surrogate = trained surrogate file: surrogate + BDF fallback
@@ -99,6 +100,7 @@ int parse_options(const char* s, Options& o) {
         else return set_err("gb.mapping must be thread or warp, got '%s'", v.c_str());
       } else if (k == "gb.wpb") o.wpb = std::stoi(v);
       else if (k == "gb.autotune") o.autotune = std::stoi(v) != 0;
+      else if (k == "gb.retry") o.retry = std::stoi(v) != 0;
       else if (k == "gb.surrogate") o.surrogate = v;
       else if (k == "gb.sg.audit") o.sg.audit_frac = std::stod(v);
       else if (k == "gb.sg.mis") o.sg.mis = std::stod(v);
@@ -191,6 +193,10 @@ struct Scratch {
   size_t audit_cap = 0;
   unsigned long long* d_sg_counts = nullptr;  // fallback count, audit count, seed
   pgb::SurrogateStats* d_sg_stats = nullptr;
+  // cells the mixed-precision pass failed, integrated again by the FP64 pass
+  void* d_retry = nullptr;
+  size_t retry_cap = 0;
+  unsigned long long* d_retry_count = nullptr;
   cudaEvent_t done = nullptr;
   long long last_ncell = 0;
   // graph cache
@@ -230,6 +236,8 @@ void free_scratch(Scratch& s) {
   if (s.d_audit) cudaFree(s.d_audit);
   if (s.d_sg_counts) cudaFree(s.d_sg_counts);
   if (s.d_sg_stats) cudaFree(s.d_sg_stats);
+  if (s.d_retry) cudaFree(s.d_retry);
+  if (s.d_retry_count) cudaFree(s.d_retry_count);
   if (s.done) cudaEventDestroy(s.done);
   s = Scratch();
 }
@@ -239,6 +247,7 @@ int ensure_scratch(pgb_reactor* r, cudaStream_t st, size_t nbox, Scratch** out) 
   if (!s.d_counter) {
     PGB_CUDA(cudaMalloc(&s.d_counter, sizeof(unsigned long long)));
     PGB_CUDA(cudaMalloc(&s.d_stats, sizeof(pgb::ReactStats)));
+    PGB_CUDA(cudaMalloc(&s.d_retry_count, sizeof(unsigned long long)));
     PGB_CUDA(cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming));
     if (r->sg.d_net) {
       PGB_CUDA(cudaMalloc(&s.d_sg_counts, 3 * sizeof(unsigned long long)));
@@ -278,14 +287,17 @@ bool use_warp(const pgb_reactor* r);
 
 // First layout (all shared; global Nordsieck history; global history and LU) whose shared
 // footprint fits 128 threads per block (the occupancy that measures best), unless options
-// force the layout or the block size.
-LaunchPlan plan_launch(const pgb_reactor* r, long long ncell) {
+// force the layout or the block size. `mixed` selects the precision planned for (the FP64
+// retry pass plans FP64 whatever gb.precision says, and then ignores a gb.wpb that does not
+// fit FP64's shared memory).
+LaunchPlan plan_launch(const pgb_reactor* r, long long ncell, bool mixed) {
   LaunchPlan pl;
   const MechEntry& m = *r->mech;
   if (use_warp(r)) {
     // warp per cell: as many warps per block as fit shared memory (or gb.wpb), one block per SM
-    const int per = r->opt.mixed ? m.wsmem_mixed : m.wsmem_fp64;
+    const int per = mixed ? m.wsmem_mixed : m.wsmem_fp64;
     int wpb = r->opt.wpb;
+    if (wpb > 0 && mixed != r->opt.mixed && wpb * per > kMaxSmemPerBlock) wpb = 0;
     if (wpb <= 0) {  // most preferred compiled size whose shared memory fits
       for (int i = 0; i < 4 && m.wpb_choice[i] > 0; ++i) {
         wpb = m.wpb_choice[i];
@@ -297,8 +309,8 @@ LaunchPlan plan_launch(const pgb_reactor* r, long long ncell) {
     pl.nblocks = (int)std::min<long long>(r->nsm, std::max<long long>(1, (ncell + wpb - 1) / wpb));
     return pl;
   }
-  const int per[3] = {r->opt.mixed ? m.smem_mixed : m.smem_fp64, r->opt.mixed ? m.smem_mixed_g : m.smem_fp64_g,
-                      r->opt.mixed ? m.smem_mixed_gl : m.smem_fp64_gl};
+  const int per[3] = {mixed ? m.smem_mixed : m.smem_fp64, mixed ? m.smem_mixed_g : m.smem_fp64_g,
+                      mixed ? m.smem_mixed_gl : m.smem_fp64_gl};
   const int tpb = r->opt.tpb > 0 ? r->opt.tpb : 128;
   int choice = -1;
   for (int c = 0; c < 3 && choice < 0; ++c) {
@@ -317,7 +329,7 @@ LaunchPlan plan_launch(const pgb_reactor* r, long long ncell) {
   const int N = m.ns + 1;
   const size_t slots = (size_t)pl.nblocks * pl.tpb;
   if (pl.z_global) pl.z_bytes = slots * (pgb::QMAX + 2) * N * sizeof(double);
-  if (pl.lu_global) pl.lu_bytes = slots * N * N * (r->opt.mixed ? sizeof(float) : sizeof(double));
+  if (pl.lu_global) pl.lu_bytes = slots * N * N * (mixed ? sizeof(float) : sizeof(double));
   return pl;
 }
 
@@ -376,12 +388,37 @@ int enqueue_advance(pgb_reactor* r, Scratch& s, int nbox, long long ncell, doubl
     const long long nb = std::min<long long>((ncell + 255) / 256, (long long)r->nsm * 8);
     return r->mech->null_fn(p, st, (int)nb);
   }
-  const LaunchPlan pl = plan_launch(r, ncell);
+  const LaunchPlan pl = plan_launch(r, ncell, r->opt.mixed);
   p.lu_scratch = pl.lu_bytes ? s.d_lu : nullptr;
   p.z_scratch = pl.z_bytes ? s.d_z : nullptr;
   LaunchFn fn = pl.warp ? (r->opt.mixed ? r->mech->warp_mixed : r->mech->warp_fp64)
                         : (r->opt.mixed ? r->mech->bdf_mixed : r->mech->bdf_fp64);
-  if (!r->sg.d_net) return fn(p, pl.tpb, st, pl.nblocks);
+  // mixed precision with retry: the cells its pass fails (FP32 Newton matrices can stall where
+  // FP64 ones converge) are listed on the device and integrated again from their untouched
+  // inputs by the FP64 kernel, on the same stream (and in the same graph)
+  const bool retry = r->opt.mixed && r->opt.retry && s.d_retry && s.d_retry_count &&
+                     (long long)(s.retry_cap / sizeof(long long)) >= ncell;
+  if (retry) {
+    p.retry_list = static_cast<long long*>(s.d_retry);
+    p.retry_count = s.d_retry_count;
+    PGB_CUDA(cudaMemsetAsync(s.d_retry_count, 0, sizeof(unsigned long long), st));
+  }
+  auto run_bdf = [&]() -> int {
+    if (fn(p, pl.tpb, st, pl.nblocks)) return -1;
+    if (!retry) return 0;
+    const LaunchPlan p64 = plan_launch(r, ncell, false);
+    pgb::ReactParams q = p;
+    q.cell_list = p.retry_list;
+    q.ncell_dev = p.retry_count;
+    q.retry_list = nullptr;
+    q.retry_count = nullptr;
+    q.lu_scratch = p64.lu_bytes ? s.d_lu : nullptr;
+    q.z_scratch = p64.z_bytes ? s.d_z : nullptr;
+    PGB_CUDA(cudaMemsetAsync(s.d_counter, 0, sizeof(unsigned long long), st));
+    const LaunchFn f64 = p64.warp ? r->mech->warp_fp64 : r->mech->bdf_fp64;
+    return f64(q, p64.tpb, st, p64.nblocks);
+  };
+  if (!r->sg.d_net) return run_bdf();
 
   // surrogate for every cell; the cells it does not accept (and the audit sample) go to the
   // BDF through the device list, then the audit compares
@@ -407,7 +444,7 @@ int enqueue_advance(pgb_reactor* r, Scratch& s, int nbox, long long ncell, doubl
   if (r->mech->sg_fn(sp, st, (int)std::min<long long>(ntiles, r->nsm))) return -1;
   p.cell_list = sp.fallback_list;
   p.ncell_dev = sp.fallback_count;
-  if (fn(p, pl.tpb, st, pl.nblocks)) return -1;
+  if (run_bdf()) return -1;
   return r->mech->sg_audit_fn(sp, st, r->nsm);
 }
 
@@ -610,7 +647,7 @@ int run_autotune(pgb_reactor* r, const std::vector<pgb::BoxDev>& boxes, long lon
     for (const Cand& c : cands) {
       r->opt.mapping = c.mapping;
       r->opt.wpb = c.wpb;
-      const LaunchPlan pl = plan_launch(r, nsample);
+      const LaunchPlan pl = plan_launch(r, nsample, r->opt.mixed);
       if (ensure_buf(sc, sc.d_z, sc.z_cap, pl.z_bytes) || ensure_buf(sc, sc.d_lu, sc.lu_cap, pl.lu_bytes)) { rc = -1; break; }
       float ms = 0.f;
       for (int rep_i = 0; rep_i < 2 && !rc; ++rep_i) {  // warm-up launch, then the timed one
@@ -653,7 +690,13 @@ int advance_box_table(pgb_reactor* r, const std::vector<pgb::BoxDev>& boxes, lon
   Scratch* s = nullptr;
   if (ensure_scratch(r, st, std::max(nbox, 1), &s)) return -1;
   if (!r->null_reactor) {
-    const LaunchPlan pl = plan_launch(r, ncell);
+    LaunchPlan pl = plan_launch(r, ncell, r->opt.mixed);
+    if (r->opt.mixed && r->opt.retry) {  // the FP64 retry pass shares the global scratch
+      const LaunchPlan p64 = plan_launch(r, ncell, false);
+      pl.z_bytes = std::max(pl.z_bytes, p64.z_bytes);
+      pl.lu_bytes = std::max(pl.lu_bytes, p64.lu_bytes);
+      if (ensure_buf(*s, s->d_retry, s->retry_cap, std::max<long long>(ncell, 1) * sizeof(long long))) return -1;
+    }
     if (ensure_buf(*s, s->d_z, s->z_cap, pl.z_bytes) || ensure_buf(*s, s->d_lu, s->lu_cap, pl.lu_bytes))
       return -1;
     if (r->sg.d_net) {
@@ -759,6 +802,7 @@ int pgb_reactor_get_stats(pgb_reactor* r, pgb_stats* out) {
   out->nst = h.nst; out->nfe = h.nfe; out->nje = h.nje; out->netf = h.netf; out->ncfn = h.ncfn;
   out->nfail = h.nfail; out->max_nst = h.max_nst;
   for (int i = 0; i < 16; ++i) out->hist[i] = h.hist[i];
+  out->nretry = h.nretry;
   return 0;
 }
 

@@ -43,6 +43,7 @@ struct ReactStats {
   unsigned long long nst, nfe, nje, netf, ncfn, nfail;
   unsigned long long max_nst;
   unsigned long long hist[16];  // steps per cell, bins [2^b, 2^(b+1))
+  unsigned long long nretry;    // cells handed to the retry list (their work is in nst/nfe/...)
 };
 
 struct ReactParams {
@@ -63,6 +64,11 @@ struct ReactParams {
   // (the surrogate's fallback cells) without a host round trip.
   const long long* cell_list;
   const unsigned long long* ncell_dev;
+  // Optional retry list (null: a failed cell writes its state at failure and its -status to
+  // FC): a cell whose integration fails appends its flat index here and leaves every caller
+  // array as it found it, so a second pass (FP64 after mixed precision) can start it over.
+  long long* retry_list;
+  unsigned long long* retry_count;
 };
 
 }  // namespace pgb

@@ -83,7 +83,7 @@ def main():
                       "ms": times, "cells_per_s": args.cells / (min(times) / 1e3),
                       "nfe_per_cell": st["nfe"] / args.cells, "nst_per_cell": st["nst"] / args.cells,
                       "nje_per_cell": st["nje"] / args.cells,
-                      "nfail": st["nfail"]}))
+                      "nfail": st["nfail"], "nretry": st["nretry"]}))
 
 
 if __name__ == "__main__":

@@ -120,7 +120,8 @@ class ReactorGB:
         s = Stats()
         check(lib().pgb_reactor_get_stats(self._h, C.byref(s)), "get_stats")
         return {"ncell": s.ncell, "nst": s.nst, "nfe": s.nfe, "nje": s.nje, "netf": s.netf,
-                "ncfn": s.ncfn, "nfail": s.nfail, "max_nst": s.max_nst, "hist": list(s.hist)}
+                "ncfn": s.ncfn, "nfail": s.nfail, "max_nst": s.max_nst, "hist": list(s.hist),
+                "nretry": s.nretry}
 
     def tuning(self) -> str:
         """The autotuner's report (gb.autotune=1), empty before the first advance."""

@@ -170,3 +170,73 @@ def test_autotuner_picks_a_compiled_mapping_and_leaves_inputs_alone(native_lib, 
     (b, _) = _run(torch, cfg, cs, [16] * 4, "gb.precision=mixed " + explicit)
     for x, y in zip(a, b):
         assert np.array_equal(x, y)
+
+
+def _run_graph_twice(torch, cfg, cs, sides, opts):
+    """Two advances of fresh copies of the same cells through one cached CUDA graph."""
+    stream = torch.cuda.Stream()
+    r = ReactorBase.create("ReactorCvode", cfg.mech, f"ode.rtol={cfg.rtol} ode.atol={cfg.atol} gb.graph=1 {opts}")
+    r.init(2, 1)
+    outs = []
+    for _ in range(2):
+        boxes = boxes_from_cells(torch, cs, sides)
+        with torch.cuda.stream(stream):
+            r.react_boxes(boxes, cfg.dt, 0.0, stream=stream)
+        stream.synchronize()
+        outs.append((gather(boxes, cs.rY.shape[1]), r.stats()))
+    r.close()
+    return outs
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("cfgname,mapping", [("lidryer_amr120", "thread"), ("drm19_2M", "warp")])
+def test_mixed_precision_retries_failed_cells_in_fp64(native_lib, cuda, cfgname, mapping):
+    """gb.retry (on by default in mixed precision): a cell the mixed-precision pass fails is
+    integrated again, from its untouched inputs, by the FP64 kernel in the same call (and the
+    same CUDA graph). A step limit below the cells' step counts makes failures certain: each
+    retried cell then equals the plain FP64 run bit for bit, every other cell the mixed run
+    without retry, and the counters split into nretry (handed over) and nfail (failed in FP64)."""
+    torch = cuda
+    cfg = CONFIGS[cfgname]
+    cs = make_cells(cfg, 4096, seed=12)
+    lim = f"gb.mapping={mapping} ode.max_steps=40"
+    (a, sa) = _run(torch, cfg, cs, [16], f"{lim} gb.precision=mixed gb.retry=0")
+    (d, sd) = _run(torch, cfg, cs, [16], f"{lim} gb.precision=fp64")
+    failed = a[3] < 0
+    assert 0 < failed.sum() < failed.size and sa["nretry"] == 0 and sa["nfail"] == failed.sum()
+    for (g, sg) in _run_graph_twice(torch, cfg, cs, [16], f"{lim} gb.precision=mixed"):
+        for x, y, z in zip(g, a, d):
+            assert np.array_equal(x[~failed], y[~failed])
+            assert np.array_equal(x[failed], z[failed])
+        assert sg["nretry"] == failed.sum()
+        assert sg["nfail"] == (d[3][failed] < 0).sum()
+    _report(f"retry[{cfgname}]", {"cells": int(failed.size), "mixed_failed": int(failed.sum()),
+                                  "failed_after_fp64_retry": int(sg["nfail"]), "fp64_alone_failed": int(sd["nfail"])})
+
+
+@pytest.mark.gpu
+def test_gri_mixed_with_retry_fails_no_more_cells_than_fp64(native_lib, cuda):
+    """On the GRI-shaped workload a few cells per 10^4 fail the FP32-Newton mixed pass (and a
+    similar number fail in FP64, as they do in the oracle). The sample holds such cells; with
+    the retry the mixed advance fails only cells that FP64 fails as well."""
+    torch = cuda
+    cfg = CONFIGS["gri_1M"]
+    full = make_cells(cfg, 65536, seed=0)
+    known = [480, 728, 7950, 9836, 12643, 13753, 15664, 15833, 18082, 19744, 25373, 29068, 30942,
+             31718, 33513, 34007, 35261, 40001, 40191, 42264, 42733, 43442, 47339, 50746, 61635, 65528]
+    rng = np.random.default_rng(9)
+    others = rng.choice(np.setdiff1d(np.arange(65536), known), 256 - len(known), replace=False)
+    sel = np.sort(np.concatenate([known, others]))
+    cs = type(full)(**{k: (v[sel] if isinstance(v, np.ndarray) and v.shape[:1] == (65536,) else v)
+                       for k, v in full.__dict__.items()})
+    shape = [(16, 16, 1)]
+    (a, sa) = _run(torch, cfg, cs, shape, "gb.precision=mixed gb.retry=0")
+    (d, sd) = _run(torch, cfg, cs, shape, "gb.precision=fp64")
+    (g, sg) = _run(torch, cfg, cs, shape, "gb.precision=mixed")
+    failed = a[3] < 0
+    for x, y, z in zip(g, a, d):
+        assert np.array_equal(x[~failed], y[~failed]) and np.array_equal(x[failed], z[failed])
+    assert sg["nretry"] == failed.sum() and sg["nfail"] == (d[3][failed] < 0).sum()
+    assert sg["nfail"] <= min(sa["nfail"], sd["nfail"])
+    _report("retry[gri_1M]", {"cells": 256, "mixed_failed": int(sa["nfail"]), "fp64_failed": int(sd["nfail"]),
+                              "mixed_with_retry_failed": int(sg["nfail"])})
