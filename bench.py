@@ -342,6 +342,9 @@ def run_gb(args, ws, rank, local, pg):
                                    "nfe_per_step": st64["nfe"]}
             r64.close()
 
+    if rank == 0 and cfg.mech != "gri_syn":
+        extra["rate_evaluation"] = rates_roofline(torch, cfg, cs, stream, flops_rhs, fp64_peak)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(cfg, cs, args.cpu_sample or default_cpu_sample(cfg))
@@ -378,12 +381,42 @@ def run_gb(args, ws, rank, local, pg):
                       "nje_per_cell": st["nje"] / ncell, "max_steps_cell": st["max_nst"], "nfail": int(st["nfail"]), "nretry": int(st["nretry"]),
                       "steps_hist_log2": hist},
             "clocks": clocks,
-            "gpu_launches": args.steps * (3 if surrogate else 1),
+            # per step: [surrogate] + BDF (+ FP64 retry pass in mixed precision) + [audit]
+            "gpu_launches": args.steps * ((2 if surrogate else 0) + (2 if args.precision == "mixed" else 1)),
             **extra,
         }
         if cpu:
             line["cpu_baseline"] = cpu
         print(json.dumps(line), flush=True)
+
+
+def rates_roofline(torch, cfg, cs, stream, flops_rhs, fp64_peak, reps=5):
+    """Instantaneous production rates (reactionRateRhoY: T from (rho h, Y), then omega-dot) of
+    every cell of the workload in one launch of `rates_kernel`, MKS in/out, CUDA-event timed."""
+    import numpy as np
+    from pelelm_gb300.reactor import reaction_rates
+    n, ns = cs.T.size, cs.rY.shape[1]
+    rY = torch.tensor(np.ascontiguousarray(cs.rY.T) * 1e3, device="cuda").view(ns, 1, 1, n)
+    rH = torch.tensor(cs.rE * 0.1, device="cuda").view(1, 1, 1, n)
+    T = torch.tensor(cs.T, device="cuda").view(1, 1, 1, n)
+    out = torch.empty_like(rY)
+    box = ((0, 0, 0), (n - 1, 0, 0))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        for _ in range(3):
+            reaction_rates(cfg.mech, box, rY, rH, T, None, out, stream=stream)
+        e0.record(stream)
+        for _ in range(reps):
+            reaction_rates(cfg.mech, box, rY, rH, T, None, out, stream=stream)
+        e1.record(stream)
+    torch.cuda.synchronize()
+    t = e0.elapsed_time(e1) / 1e3 / reps
+    achieved = flops_rhs * n / t / 1e12
+    return {"kernel": "rates_kernel", "cells": n, "ms_per_launch": 1e3 * t, "cells_per_s": n / t,
+            "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s", "frac": achieved / fp64_peak,
+            "what": f"{flops_rhs} counted FP64 flops per cell (one RHS); the T-from-(rho h, Y) Newton "
+                    "iterations before the rates are executed but not counted",
+            "bytes_per_cell": 8 * (2 * ns + 2), "inputs_vs_l2": "inputs larger than L2"}
 
 
 WORKLOAD_TEXT = {
