@@ -366,6 +366,7 @@ __device__ __noinline__ bool warp_setup(const WVec<M> yv, const double gamma, co
       const int k = idx(cc);
       if (k > NS) continue;
       JR acc = JR(0);
+#pragma unroll 1
       for (int i = 0; i < NS; ++i) acc += TH_[i] * RT * Tab::template sp<JR>(i).invW * A[i * LDA + k];
       if (k < NS) {
         A[NS * LDA + k] = -acc * invD - QD2 * TC[k] * JR(kRerg) * Tab::template sp<JR>(k).invW;
@@ -384,6 +385,7 @@ __device__ __noinline__ bool warp_setup(const WVec<M> yv, const double gamma, co
       if (k < N) A[e] = (i == k ? JR(1) : JR(0)) - g * A[e];
     }
     __syncwarp();
+#pragma unroll 1
     for (int k = 0; k < N; ++k) {
       // pivot: first row of largest |a_ik|, i >= k
       JR best = JR(-1);
@@ -419,6 +421,7 @@ __device__ __noinline__ bool warp_setup(const WVec<M> yv, const double gamma, co
         if (i > k && i < N) {
           const JR l = A[i * LDA + k] * inv;
           A[i * LDA + k] = l;
+#pragma unroll 4
           for (int j = k + 1; j < N; ++j) A[i * LDA + j] -= l * A[k * LDA + j];
         }
       }
@@ -490,6 +493,7 @@ __global__ void __launch_bounds__(WPB * 32, 1) bdf_warp_kernel(const ReactParams
     for (int r = 0; r < R; ++r)
       if (idx(r) < N) XS[idx(r)] = (JR)b[r];
     __syncwarp();
+#pragma unroll 1
     for (int k = 0; k < N; ++k) {
       const int p = PIV[k];
       if (p != k && lane == 0) { const JR tmp = XS[k]; XS[k] = XS[p]; XS[p] = tmp; }
@@ -502,6 +506,7 @@ __global__ void __launch_bounds__(WPB * 32, 1) bdf_warp_kernel(const ReactParams
       }
       __syncwarp();
     }
+#pragma unroll 1
     for (int k = N - 1; k >= 0; --k) {
       const JR xk = XS[k] * A[k * LDA + k];
       __syncwarp();
