@@ -371,7 +371,8 @@ def run_gb(args, ws, rank, local, pg):
                          "frac": achieved / fp64_peak,
                          # DRAM bytes per launch from an ncu capture of a smaller launch of the same
                          # kernel, scaled by cells (profiles/)
-                         "traffic": TRAFFIC_PER_CELL.get(cfg.mech, 0.0) * ncell if not surrogate else None,
+                         "traffic": (TRAFFIC_PER_CELL[cfg.mech] * (sst["fallback"] if surrogate else ncell)
+                                     if cfg.mech in TRAFFIC_PER_CELL else None),
                          "kernel": dominant,
                          "what": f"rate evaluation: {flops_rhs} algorithmic FP64 flops per RHS "
                                  f"({ops} ops + {trans} transcendentals x {FLOPS_PER_TRANSCENDENTAL}) "
@@ -430,8 +431,9 @@ WORKLOAD_TEXT = {
                 "96x32^3 + 256x16^3 = 2^22 cells, dt_react 1e-5 s, rtol 1e-6, atol 1e-10",
 }
 
-# DRAM bytes per cell of one BDF launch (ncu, scaled from the captured launch)
-TRAFFIC_PER_CELL = {"lidryer_syn": 22.81e6 / 131072}
+# DRAM bytes per cell of one BDF launch (dram__bytes_read.sum + dram__bytes_write.sum of an ncu
+# capture of a smaller launch of the same kernel, divided by its cells; profiles/)
+TRAFFIC_PER_CELL = {"lidryer_syn": 22.81e6 / 131072, "drm19_syn": (12.074496e6 + 0.054272e6) / 32768}
 
 
 def measured_peaks():

@@ -1,0 +1,52 @@
+"""GPU reactor on the states of the reference's own flame profiles (cold reactants, preheat and
+radical-rich reaction zone, burnt gas; tests/golden/flame_states.npz), no forcing, against the
+CPU oracle through the C ABI: FP64 at the plain tolerances on both mappings, mixed precision by
+its error against an rtol-1e-11 oracle (no worse than the FP64 oracle's own at rtol 1e-6)."""
+import numpy as np
+import pytest
+
+from helpers import boxes_from_cells, gather, tol_ratio
+from pelelm_gb300.reactor import ReactorBase
+from pelelm_gb300.workloads import CONFIGS, CellState, mech_path
+from test_flame_states import G, flame_cells
+
+
+def _cells(cfgname):
+    rY, T, rE = flame_cells(cfgname)
+    n = T.size
+    return CellState(rY=rY, rYsrc=np.zeros_like(rY), T=T.copy(), rE=rE, rEsrc=np.zeros(n),
+                     mask=np.ones(n, dtype=np.int32), p=np.zeros(n))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("cfgname", ["lidryer_amr120", "drm19_2M"])
+@pytest.mark.parametrize("opts", ["gb.mapping=thread gb.precision=fp64", "gb.mapping=warp gb.precision=fp64",
+                                  "gb.precision=mixed"])
+def test_flame_profile_states_against_oracle(native_lib, oracle_mod, cuda, cfgname, opts):
+    torch = cuda
+    cfg = CONFIGS[cfgname]
+    cs = _cells(cfgname)
+    n = cs.T.size
+    boxes = boxes_from_cells(torch, cs, [(n, 1, 1)])
+    r = ReactorBase.create("ReactorCvode", cfg.mech, f"ode.rtol={cfg.rtol} ode.atol={cfg.atol} {opts}")
+    r.init(2, 1)
+    r.react_boxes(boxes, cfg.dt, 0.0)
+    torch.cuda.synchronize()
+    st = r.stats()
+    r.close()
+    rYg, Tg, rEg, FCg = gather(boxes, cs.rY.shape[1])
+    om = oracle_mod.OracleMech(mech_path(cfg.mech))
+    rYo, To, rEo, FCo, nf = om.react(cs.rY, cs.rYsrc, cs.T, cs.rE, cs.rEsrc, cs.mask, cfg.dt, cfg.rtol, cfg.atol)
+    assert st["nfail"] == 0 and nf == 0 and np.all(FCg > 0)
+    np.testing.assert_array_equal(rEg, cs.rE)  # no forcing: rho h is carried exactly
+    if "fp64" in opts:
+        within = (np.abs(Tg - To) / To <= 1e-6) & (tol_ratio(rYg, rYo, cfg.rtol, cfg.atol).max(1) <= 1.0)
+        assert within.mean() >= 0.99, within.mean()
+    else:
+        tight = om.react(cs.rY, cs.rYsrc, cs.T, cs.rE, cs.rEsrc, cs.mask, cfg.dt, 1e-11, 1e-16, max_steps=200000)
+        eg, eo = np.abs(Tg - tight[1]).max(), np.abs(To - tight[1]).max()
+        assert eg <= 2.0 * eo + 50 * cfg.rtol * float(tight[1].max()), (eg, eo)
+        Yt = tight[0] / tight[0].sum(1, keepdims=True)
+        eg = np.abs(rYg / rYg.sum(1, keepdims=True) - Yt).max()
+        eo = np.abs(rYo / rYo.sum(1, keepdims=True) - Yt).max()
+        assert eg <= 2.0 * eo + 50 * cfg.rtol, (eg, eo)
