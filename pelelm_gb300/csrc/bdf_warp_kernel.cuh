@@ -387,25 +387,50 @@ __device__ __noinline__ bool warp_setup(const WVec<M> yv, const double gamma, co
     __syncwarp();
 #pragma unroll 1
     for (int k = 0; k < N; ++k) {
-      // pivot: first row of largest |a_ik|, i >= k
-      JR best = JR(-1);
-      int bi = N;
+      // pivot: first row of largest |a_ik|, i >= k (NaN never wins; none above 0: singular)
+      int p = N;
+      if constexpr (sizeof(JR) == sizeof(float)) {
+        // a non-negative float orders as its bit pattern: one warp max-reduction, then the
+        // lowest row holding the maximum from the lane ballots (rows lane + 32 r, r ascending)
+        unsigned bits[R], m = 0u;
 #pragma unroll
-      for (int r = 0; r < R; ++r) {
-        const int i = idx(r);
-        if (i >= k && i < N) {
-          const JR v = fabs(A[i * LDA + k]);
-          if (v > best) { best = v; bi = i; }
+        for (int r = 0; r < R; ++r) {
+          const int i = idx(r);
+          unsigned b = 0u;
+          if (i >= k && i < N) {
+            const float v = fabsf(A[i * LDA + k]);
+            if (v == v) b = __float_as_uint(v);
+          }
+          bits[r] = b;
+          m = max(m, b);
         }
-      }
+        m = __reduce_max_sync(0xffffffffu, m);
+        if (m == 0u) return false;
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        const JR ob = __shfl_xor_sync(0xffffffffu, best, o);
-        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-        if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+        for (int r = 0; r < R; ++r) {
+          const unsigned bal = __ballot_sync(0xffffffffu, bits[r] == m);
+          if (p == N && bal) p = 32 * r + __ffs(bal) - 1;
+        }
+      } else {
+        JR best = JR(-1);
+        int bi = N;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          const int i = idx(r);
+          if (i >= k && i < N) {
+            const JR v = fabs(A[i * LDA + k]);
+            if (v > best) { best = v; bi = i; }
+          }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          const JR ob = __shfl_xor_sync(0xffffffffu, best, o);
+          const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+          if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+        }
+        if (!(best > JR(0))) return false;
+        p = bi;
       }
-      if (!(best > JR(0))) return false;
-      const int p = bi;
       if (lane == 0) PIV[k] = p;
       if (p != k)
         for (int j = k + lane; j < N; j += 32) {
