@@ -197,6 +197,8 @@ int pgb_rhoh_to_temp(const char* mechanism, const pgb_box_view* view, double tmi
  *   (the queue head and counters are cleared on each call). Calls whose work overlaps on the
  *   GPU — concurrent streams or threads — race on it: serialize them.
  * - Stream ordered; if stats is non-NULL the call waits for the advance and fills it.
+ * - No FP64 retry pass (it would need a failed-cell list sized by the cell count): a cell that
+ *   fails keeps its state at failure and FC = -status, as with gb.retry=0.
  * Returns 0 on success, -1 on error (pgb_last_error). */
 #define PGB_NOALLOC_MAX_BOXES 1024
 int pgb_react_boxes_noalloc(const char* mechanism, const pgb_box_view* views, int nbox,
