@@ -436,4 +436,15 @@ BdfStats bdf_integrate(const Mechanism& m, double* y, const double* F, double Fh
   return b.st;
 }
 
+bool lu_solve(int n, const double* A, const double* b, double* x) {
+  Lu lu;
+  lu.n = n;
+  lu.a.assign(A, A + (size_t)n * n);
+  lu.piv.assign(n, 0);
+  if (!lu.factor()) return false;
+  for (int i = 0; i < n; ++i) x[i] = b[i];
+  lu.solve(x);
+  return true;
+}
+
 }  // namespace orc

@@ -91,4 +91,8 @@ struct BdfStats {
 BdfStats bdf_integrate(const Mechanism& m, double* y, const double* F, double Fh, double dt,
                        const BdfOptions& opt);
 
+// The integrator's dense partial-pivot LU applied to one system A x = b (A row-major n x n);
+// false when a pivot column is zero (singular). For the LU known-answer tests.
+bool lu_solve(int n, const double* A, const double* b, double* x);
+
 }  // namespace orc

@@ -23,8 +23,8 @@ _lp = C.POINTER(C.c_long)
 
 
 def build(force: bool = False) -> str:
-    if force or not os.path.exists(LIB_PATH):
-        subprocess.check_call(["make", "-s", "-C", HERE])
+    """make (incremental: rebuilds when a source is newer than the library)."""
+    subprocess.check_call(["make", "-s", "-C", HERE] + (["-B"] if force else []))
     return LIB_PATH
 
 
@@ -55,6 +55,8 @@ def lib():
         L.orc_bdf_one.argtypes = [C.c_void_p, _dp, _dp, C.c_double, C.c_double, C.c_double, _dp,
                                   C.c_int, C.c_int, _lp]
         L.orc_max_threads.restype = C.c_int
+        L.orc_lu_solve.restype = C.c_int
+        L.orc_lu_solve.argtypes = [C.c_int, _dp, _dp, _dp]
         _lib = L
     return _lib
 
@@ -152,3 +154,11 @@ class OracleMech:
 
 def max_threads() -> int:
     return lib().orc_max_threads()
+
+
+def lu_solve(A, b):
+    """The integrator's partial-pivot LU on one system; returns x, or None when singular."""
+    A = np.ascontiguousarray(A, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    x = np.empty_like(b)
+    return None if lib().orc_lu_solve(A.shape[0], _d(A), _d(b), _d(x)) else x

@@ -144,4 +144,10 @@ int orc_bdf_one(void* h, double* y, const double* F, double Fh, double dt, doubl
   return st.status;
 }
 
+// Dense partial-pivot LU solve of one system with the integrator's factorisation; 0 ok,
+// 1 singular.
+int orc_lu_solve(int n, const double* A, const double* b, double* x) {
+  return orc::lu_solve(n, A, b, x) ? 0 : 1;
+}
+
 }  // extern "C"

@@ -188,3 +188,37 @@ def test_op_count_model_matches_counting_oracle(oracle_mod):
         om = oracle_mod.OracleMech(mech_path(mech))
         y = np.append(np.full(m.ns, 1e-5), 1500.0)
         assert om.count_rhs(y, np.zeros(m.ns), 0.0) == rhs_ops(m)
+
+
+def test_lu_known_answers(oracle_mod):
+    """The integrator's partial-pivot LU: residuals at round-off on random systems of the three
+    mechanisms' sizes and on Newton matrices I - gamma J of a real cell, exact answers where
+    pivoting is forced (zero diagonal), and singular matrices reported."""
+    rng = np.random.default_rng(17)
+    for n in (10, 22, 54):
+        A = rng.normal(size=(n, n)) + n * np.eye(n) * rng.uniform(0.0, 1.0)
+        b = rng.normal(size=n)
+        x = oracle_mod.lu_solve(A, b)
+        assert np.linalg.norm(A @ x - b) <= 1e-13 * np.linalg.norm(A) * np.linalg.norm(x)
+        np.testing.assert_allclose(x, np.linalg.solve(A, b), rtol=1e-9, atol=1e-12 * np.abs(x).max())
+    # a permutation with a zero diagonal: exact
+    P = np.eye(6)[[3, 0, 5, 1, 2, 4]]
+    assert np.all(np.diag(P) == 0.0)
+    b = np.arange(1.0, 7.0)
+    np.testing.assert_array_equal(oracle_mod.lu_solve(P, b), P.T @ b)
+    # a zero column, and an all-zero matrix: singular
+    S = rng.normal(size=(5, 5))
+    S[:, 2] = 0.0
+    assert oracle_mod.lu_solve(S, np.ones(5)) is None
+    assert oracle_mod.lu_solve(np.zeros((3, 3)), np.ones(3)) is None
+    # Newton matrices of a drm19 cell over the step sizes the integrator takes
+    cfg = CONFIGS["drm19_2M"]
+    om = oracle_mod.OracleMech(mech_path(cfg.mech))
+    cs = make_cells(cfg, 1, seed=23)
+    y = np.append(cs.rY[0], cs.T[0])
+    J = om.jac(y, cs.rYsrc[0], cs.rEsrc[0])
+    for gamma in (1e-10, 1e-8, 1e-6):
+        M = np.eye(y.size) - gamma * J
+        b = rng.normal(size=y.size)
+        x = oracle_mod.lu_solve(M, b)
+        assert np.linalg.norm(M @ x - b) <= 1e-12 * np.linalg.norm(M) * np.linalg.norm(x)
