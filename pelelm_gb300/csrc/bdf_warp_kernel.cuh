@@ -1,5 +1,6 @@
-// Persistent, work-stealing, warp-per-cell BDF reactor kernel for mechanisms too large for one
-// cell per thread (GRI-Mech-sized: 53 species, 325 reactions, N = 54 unknowns).
+// Persistent, work-stealing, warp-per-cell BDF reactor kernel for mechanisms whose per-cell state
+// no longer fits a thread: the default for drm19-sized mechanisms (21 species, 84 reactions) and
+// the only mapping for GRI-Mech-sized ones (53 species, 325 reactions, N = 54 unknowns).
 //
 // Same contract and algorithm as bdf_kernel.cuh (the PelePhysics reactor called at
 // Source/PeleLM.cpp:5752; CVODE-class fixed-leading-coefficient variable-order Nordsieck BDF,
@@ -15,13 +16,17 @@
 //    progress, from global-memory tables read through L1: lanes read different entries), then
 //    over species again gathering their reactions (species-major lists: a deterministic order,
 //    no atomics), with warp-shuffle sums for the energy closure;
-//  * Jacobian (type JR: FP32 in mixed precision): per-reaction partials lane-parallel, then an
-//    assembly in reaction order with lanes over columns (each lane owns its columns, so the
-//    result does not depend on scheduling); constant-pressure energy row by column;
-//  * LU and triangular solves: lanes own rows; pivot search by warp arg-max; matrix rows padded
-//    to N+1 so a column access is bank-conflict free;
+//  * Jacobian (type JR: FP32 in mixed precision): NASA-7 terms once per species, per-reaction
+//    partials lane-parallel, then an assembly in reaction order with lanes over columns (each
+//    lane owns its columns, so the result does not depend on scheduling); constant-pressure
+//    energy row by column;
+//  * LU and triangular solves: lanes own rows; pivot search by warp arg-max (FP32: one max-
+//    reduction over the |a| bit patterns); matrix rows padded to N+1 so a column access is
+//    bank-conflict free;
 //  * per-warp state (Nordsieck history, forcing, rates, matrix) in shared memory; a warp takes
-//    the next cell index with one atomic when its cell is done (work stealing across all boxes).
+//    the next cell index with one atomic when its cell is done (work stealing across all boxes);
+//  * with a retry list (mixed precision), a failed cell is listed and left untouched for the
+//    FP64 pass that follows on the same stream.
 #ifndef PGB_BDF_WARP_KERNEL_CUH
 #define PGB_BDF_WARP_KERNEL_CUH
 
