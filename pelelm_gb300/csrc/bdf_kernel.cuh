@@ -20,6 +20,8 @@
 //  * Nordsieck history, forcing and the LU live in shared memory laid out
 //    [element][thread] (each warp access is contiguous, bank-conflict free); the state,
 //    correction and error weights live in registers (N is a compile-time constant).
+//  * With a retry list (mixed precision), a cell whose integration fails is listed and its
+//    arrays are left as they were, for the FP64 pass that follows on the same stream.
 #ifndef PGB_BDF_KERNEL_CUH
 #define PGB_BDF_KERNEL_CUH
 
