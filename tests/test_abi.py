@@ -51,6 +51,7 @@ def test_version_and_mechanisms(native_lib):
     ("ReactorCvode", "lidryer_syn", 2, "cvode.solve_type=GMRES", "not provided"),
     ("ReactorCvode", "lidryer_syn", 2, "gb.precision=fp16", "gb.precision"),
     ("ReactorCvode", "lidryer_syn", 2, "foo.bar=1", "unknown option"),
+    ("ReactorCvode", "lidryer_syn", 2, "gb.retry=yes", "bad value"),
 ])
 def test_create_rejects_bad_arguments(native_lib, name, mech, rtype, opts, msg):
     from pelelm_gb300 import _lib
@@ -65,3 +66,50 @@ def test_python_factory_mirrors_reference_names():
         ReactorBase.create("ReactorArkode")
     r = ReactorBase.create("ReactorCvode", "lidryer_syn", "ode.rtol=1e-6")
     assert (r.ns, r.nr) == (9, 21)
+
+
+C_PROGRAM = r"""
+#include "pelelm_gb300.h"
+#include <stdio.h>
+#include <string.h>
+int main(void) {
+  int ns = 0, nr = 0;
+  char buf[512];
+  pgb_stats st;
+  pgb_box_view v;
+  pgb_chem_view cv;
+  pgb_reactor* r;
+  memset(&st, 0, sizeof st);
+  memset(&v, 0, sizeof v);
+  memset(&cv, 0, sizeof cv);
+  if (pgb_version() != PGB_ABI_VERSION) return 1;
+  if (pgb_mechanism_info("drm19_syn", &ns, &nr) != 0 || ns != 21 || nr != 84) return 2;
+  r = pgb_reactor_create("ReactorRK64", "drm19_syn", 2, "");
+  if (r) return 3;
+  pgb_last_error(buf, sizeof buf);
+  if (!strstr(buf, "not provided")) return 4;
+  printf("%d %d %s\n", ns, nr, buf);
+  return 0;
+}
+"""
+
+
+@pytest.mark.parametrize("compiler,std", [("gcc", "-std=c99"), ("g++", "-std=c++17")])
+def test_header_compiles_links_and_calls_from_c(native_lib, tmp_path, compiler, std):
+    """The header is plain C (and C++): a program written against it alone compiles with
+    warnings as errors, links the library and gets answers and error messages (no GPU call)."""
+    import shutil
+    import subprocess
+    if not shutil.which(compiler):
+        pytest.skip(f"{compiler} not installed")
+    from pelelm_gb300._build import LIB
+    src = tmp_path / ("abi_check.c" if compiler == "gcc" else "abi_check.cpp")
+    src.write_text(C_PROGRAM)
+    exe = tmp_path / "abi_check"
+    libdir = os.path.dirname(LIB)
+    subprocess.run([compiler, std, "-Wall", "-Wextra", "-Werror", "-I", os.path.join(ROOT, "include"),
+                    str(src), "-L", libdir, "-lpelelm_gb300", f"-Wl,-rpath,{libdir}", "-o", str(exe)],
+                   check=True, capture_output=True, text=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert out.returncode == 0, (out.returncode, out.stdout, out.stderr)
+    assert out.stdout.startswith("21 84 ")
