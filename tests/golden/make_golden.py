@@ -43,7 +43,7 @@ def vode_cell(om, y0, F, Fh, dt, rtol=1e-12, atol=1e-20):
 def main():
     out = {}
     for cfgname, n, seed in (("lidryer_32cube", 12, 101), ("lidryer_amr120", 12, 102),
-                             ("drm19_2M", 6, 103)):
+                             ("drm19_2M", 6, 103), ("gri_1M", 4, 104)):
         cfg = CONFIGS[cfgname]
         om = O.OracleMech(mech_path(cfg.mech))
         cs = make_cells(cfg, n, seed=seed)

@@ -115,7 +115,7 @@ def test_bdf_closed_form_relaxation(oracle_mod, tmp_path, reversible):
 def test_oracle_matches_vode_golden(oracle_mod):
     """Tight oracle (rtol 1e-11) against scipy VODE BDF at rtol 1e-12 (committed fixture)."""
     g = np.load(os.path.join(HERE, "golden", "vode_cells.npz"))
-    for cfgname in ("lidryer_32cube", "lidryer_amr120", "drm19_2M"):
+    for cfgname in ("lidryer_32cube", "lidryer_amr120", "drm19_2M", "gri_1M"):
         cfg = CONFIGS[cfgname]
         om = oracle_mod.OracleMech(mech_path(cfg.mech))
         y0, F, Fh, yT = (g[f"{cfgname}/{k}"] for k in ("y0", "F", "Fh", "yT"))
