@@ -429,6 +429,9 @@ WORKLOAD_TEXT = {
                 "lidryer_amr120",
     "drm19_4M": "drm19_4M: drm19-shaped CH4/air (21 sp, 84 rx), the drm19_2M state distribution on "
                 "96x32^3 + 256x16^3 = 2^22 cells, dt_react 1e-5 s, rtol 1e-6, atol 1e-10",
+    "gri_1M": "gri_1M: GRI-shaped CH4/air (53 sp, 325 rx), 2x64^3 + 14x32^3 + 14x16^3 + 16x8^3 = 2^20 cells, "
+              "T = 300 + 2100 c, phi ~ U[0.5,1.5], p ~ U[1,10] atm, dt_react 1e-5 s, rtol 1e-6, atol 1e-10, "
+              "forcing as lidryer_amr120",
 }
 
 # DRAM bytes per cell of one BDF launch (dram__bytes_read.sum + dram__bytes_write.sum of an ncu
@@ -493,7 +496,7 @@ def error_vs_oracle(cfg, cs, lay, out_state, sample):
 
 def default_cpu_sample(cfg):
     # about 10-30 s of CPU work on the box's 16 cores
-    return {"lidryer_syn": cfg.ncell, "drm19_syn": 131072}.get(cfg.mech, 65536)
+    return {"lidryer_syn": cfg.ncell, "drm19_syn": 131072, "gri_syn": 16384}.get(cfg.mech, 65536)
 
 
 # ---------------------------------------------------------------- CPU (oracle) legs
