@@ -59,6 +59,12 @@ def parse():
     p.add_argument("--no-fp64-line", action="store_true")
     p.add_argument("--cpu-sample", type=int, default=0,
                    help="cells timed on the CPU (0 = the whole workload, ~10 s on 16 cores)")
+    p.add_argument("--profile-case", action="store_true",
+                   help="small advance for ncu captures: --cells seeded cells of --config in 32^3 "
+                        "boxes, --reps advances, one JSON line with their CUDA-event times")
+    p.add_argument("--cells", type=int, default=32768)
+    p.add_argument("--reps", type=int, default=2)
+    p.add_argument("--options", default="", help="extra reactor options (profile case)")
     return p.parse_args()
 
 
@@ -558,8 +564,68 @@ def run_reference(args, ws, rank, pg):
     print(json.dumps(line), flush=True)
 
 
+def run_profile_case(args):
+    """A small reactor advance of one config, for ncu captures and quick timings: `cells` seeded
+    cells in 32^3 boxes (a remainder in one (rest, 1, 1) box), `reps` advances through the C ABI
+    from a restored state, each timed with CUDA events; prints one JSON line."""
+    import torch
+    from pelelm_gb300.reactor import BoxArrays, ReactorBase
+    from pelelm_gb300.workloads import CONFIGS, make_cells
+
+    cfg = CONFIGS[args.config]
+    n = args.cells
+    cs = make_cells(cfg, n, seed=0)
+    ns = cs.rY.shape[1]
+    side = 32
+    nfull = n // side ** 3
+    shapes = [(side, side, side)] * nfull
+    if n - nfull * side ** 3:
+        shapes.append((n - nfull * side ** 3, 1, 1))
+    off = np.cumsum([0] + [a * b * c for a, b, c in shapes])
+    fields = {"rY": (cs.rY, ns), "rY_src": (cs.rYsrc, ns), "T": (cs.T[:, None], 1),
+              "rEner": (cs.rE[:, None], 1), "rEner_src": (cs.rEsrc[:, None], 1)}
+    pristine = {k: torch.tensor(np.concatenate([a[off[b]:off[b + 1]].T.reshape(-1) for b in range(len(shapes))]),
+                                device="cuda") for k, (a, nc) in fields.items()}
+    work = {k: v.clone() for k, v in pristine.items()}
+    work["FC"] = torch.zeros(n, dtype=torch.float64, device="cuda")
+    boxes = []
+    for b, (nx, ny, nz) in enumerate(shapes):
+        c0, c1 = int(off[b]), int(off[b + 1])
+
+        def v(name, nc):
+            return work[name][c0 * nc:c1 * nc].view(nc, nz, ny, nx)
+
+        boxes.append(BoxArrays(((0, 0, 0), (nx - 1, ny - 1, nz - 1)), v("rY", ns), v("rY_src", ns),
+                               v("T", 1), v("rEner", 1), v("rEner_src", 1), v("FC", 1), None))
+    r = ReactorBase.create("ReactorCvode", cfg.mech, f"ode.rtol={cfg.rtol} ode.atol={cfg.atol} "
+                           f"gb.precision={args.precision} {args.options}")
+    r.init(2, 1)
+    stream = torch.cuda.Stream()
+    times = []
+    for _ in range(args.reps):
+        for k in pristine:
+            work[k].copy_(pristine[k])
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            r.react_boxes(boxes, cfg.dt, 0.0, stream=stream)
+            e1.record(stream)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    st = r.stats()
+    r.close()
+    print(json.dumps({"config": args.config, "cells": n, "precision": args.precision, "options": args.options,
+                      "ms": times, "cells_per_s": n / (min(times) / 1e3), "nfe_per_cell": st["nfe"] / n,
+                      "nst_per_cell": st["nst"] / n, "nje_per_cell": st["nje"] / n, "nfail": st["nfail"],
+                      "nretry": st["nretry"]}), flush=True)
+
+
 def main():
     args = parse()
+    if args.profile_case:
+        run_profile_case(args)
+        return
     ws, rank, local, pg = dist_setup(args)
     if args.impl == "reference":
         run_reference(args, ws, rank, pg)

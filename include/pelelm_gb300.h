@@ -63,7 +63,9 @@ typedef struct {
  * "ReactorRK64"/"ReactorArkode" are rejected. mechanism: a mechanism compiled into the library
  * (pgb_mechanism_info). reactor_type must be 2 (rho h, constant pressure), the value PeleLM uses.
  * options: whitespace/semicolon separated key=value pairs — the reference's runtime keys
- * ode.rtol, ode.atol, cvode.max_order, cvode.solve_type, ode.analytical_jacobian,
+ * ode.rtol, ode.atol, cvode.max_order, cvode.solve_type (dense direct solve with the analytic
+ * Jacobian; the GPU decks' matrix-free GMRES / precGMRES keys run that same Newton solve
+ * directly), ode.analytical_jacobian,
  * peleLM.use_typ_vals_chem, plus ode.max_steps, gb.precision=fp64|mixed, gb.tpb, gb.graph=0|1,
  * gb.history=shared|global, gb.lu=shared|global, gb.mapping=thread|warp, gb.wpb, gb.autotune=0|1
  * (time every compiled mapping on the first advance's cells, keep the fastest), gb.retry=0|1
@@ -187,9 +189,13 @@ int pgb_rhoh_to_temp(const char* mechanism, const pgb_box_view* view, double tmi
  * cudaMalloc, cudaFree or other allocating routine: the caller passes all inputs and outputs
  * through the box views, and the scratch (box table, work-queue head, counters) is one fixed
  * device array inside the library, about 370 KB, which every GPU that loads the library holds
- * until the process exits. It runs the same persistent work-stealing kernel as
- * pgb_reactor_react_boxes with uniform tolerances (rtol, atol), cvode.max_order = max_order,
+ * until the process exits. It runs the persistent work-stealing kernels of
+ * pgb_reactor_react_boxes with their working state in shared memory — cell per thread for the
+ * 9-species mechanism, cell per warp for the larger ones — with cvode.max_order = max_order,
  * ode.max_steps = max_steps and FP64 (fp64 != 0) or mixed (fp64 == 0) Jacobian precision.
+ * The tolerances are uniform: rtol, and atol on every component. The typical-value scaling of
+ * set_typ_vals_ode / peleLM.use_typ_vals_chem does not apply here (there is no reactor object
+ * to hold the typical values), so results equal those of a reactor created without it.
  * - nbox must be in [1, PGB_NOALLOC_MAX_BOXES]; larger box lists are rejected with an error.
  * - The first call on a device (with that device current) resolves the scratch array's device
  *   address; make that first call before any stream capture.

@@ -7,10 +7,13 @@
 // (inputs and outputs, through the box views) and keeps its own scratch — the box table, the
 // work-queue head and the counters — in one fixed file-scope device array below. It calls no
 // cudaMalloc, cudaFree or other allocating routine; it launches the same persistent
-// work-stealing kernel as pgb_reactor_react_boxes.
+// work-stealing kernels as pgb_reactor_react_boxes (cell per thread for small mechanisms, cell
+// per warp for the larger ones), with their working state in shared memory only.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <atomic>
+#include <cstring>
 
 #include "reactor_registry.cuh"
 
@@ -51,6 +54,23 @@ int scratch_of_current_device(NoAllocScratch** out) {
   return 0;
 }
 
+// Box descriptors travel to the scratch array as kernel parameters, kBoxesPerCopy at a time
+// (3.5 KB, under the classic 4 KB parameter limit): the launch copies them, so no host buffer
+// has to outlive the call and nothing pageable is referenced by the stream.
+constexpr int kBoxesPerCopy = 8;
+struct BoxChunk {
+  pgb::BoxDev b[kBoxesPerCopy];
+};
+static_assert(sizeof(BoxChunk) <= 4000, "box chunk exceeds the kernel parameter space");
+
+__global__ void store_boxes_kernel(const BoxChunk chunk, int n, pgb::BoxDev* dst) {
+  constexpr int kWords = (int)(sizeof(pgb::BoxDev) / sizeof(unsigned long long));
+  static_assert(sizeof(pgb::BoxDev) % sizeof(unsigned long long) == 0, "BoxDev is not 8-byte sized");
+  const unsigned long long* src = reinterpret_cast<const unsigned long long*>(chunk.b);
+  unsigned long long* out = reinterpret_cast<unsigned long long*>(dst);
+  for (int i = threadIdx.x; i < n * kWords; i += blockDim.x) out[i] = src[i];
+}
+
 }  // namespace
 
 extern "C" int pgb_react_boxes_noalloc(const char* mechanism, const pgb_box_view* views, int nbox,
@@ -58,7 +78,6 @@ extern "C" int pgb_react_boxes_noalloc(const char* mechanism, const pgb_box_view
                                        int max_steps, int fp64, void* stream, pgb_stats* stats) {
   const MechEntry* m = find_mech_entry(mechanism);
   if (!m) return set_err("unknown mechanism '%s'", mechanism ? mechanism : "(null)");
-  if (!m->bdf_mixed) return set_err("noalloc: mechanism '%s' has no cell-per-thread kernel", m->name);
   if (nbox < 1 || !views) return set_err("noalloc: need at least one box view");
   if (nbox > PGB_NOALLOC_MAX_BOXES)
     return set_err("noalloc: %d boxes exceed the fixed scratch capacity of %d boxes; split the "
@@ -67,29 +86,43 @@ extern "C" int pgb_react_boxes_noalloc(const char* mechanism, const pgb_box_view
     return set_err("noalloc: dt_react, rtol and atol must be > 0");
   if (max_order < 1 || max_order > pgb::QMAX) return set_err("noalloc: max_order must be in [1, %d]", pgb::QMAX);
   if (max_steps < 1) return set_err("noalloc: max_steps must be >= 1");
+  // Kernel choice, all state in shared memory: cell per thread where 64 threads' state fits a
+  // block (the LiDryer-sized mechanisms), else cell per warp with the most preferred compiled
+  // warps-per-block size that fits (drm19- and GRI-sized).
+  const int per_thread = fp64 ? m->smem_fp64 : m->smem_mixed;
+  const bool thread_ok = m->bdf_mixed && m->ns <= 12 && per_thread * 64 <= kMaxSmemPerBlock;
+  int wpb = 0;
+  if (!thread_ok) {
+    const int per_warp = fp64 ? m->wsmem_fp64 : m->wsmem_mixed;
+    for (int i = 0; i < 4 && m->wpb_choice[i] > 0 && !wpb; ++i)
+      if (m->wpb_choice[i] * per_warp <= kMaxSmemPerBlock) wpb = m->wpb_choice[i];
+    if (!wpb || !m->warp_mixed)
+      return set_err("noalloc: no compiled kernel of mechanism '%s' keeps its state in shared memory", m->name);
+  }
   NoAllocScratch* S = nullptr;
   if (scratch_of_current_device(&S)) return -1;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
 
-  // Box table: converted in small host chunks on the stack and copied into the scratch array.
-  // A pageable-source cudaMemcpyAsync has consumed the host buffer when it returns.
-  constexpr int kChunk = 16;
-  pgb::BoxDev chunk[kChunk];
+  // Box table: validated and converted here, copied into the scratch array through kernel
+  // parameters.
+  BoxChunk chunk;
   long long ncell = 0;
-  for (int b0 = 0; b0 < nbox; b0 += kChunk) {
-    const int n = (nbox - b0 < kChunk) ? nbox - b0 : kChunk;
+  for (int b0 = 0; b0 < nbox; b0 += kBoxesPerCopy) {
+    const int n = (nbox - b0 < kBoxesPerCopy) ? nbox - b0 : kBoxesPerCopy;
     for (int i = 0; i < n; ++i) {
       const pgb_box_view& v = views[b0 + i];
-      if (fill_box_dev(v, m->ns, ncell, b0 + i, chunk[i])) return -1;
-      ncell += (long long)chunk[i].len0 * chunk[i].len1 * chunk[i].len2;
+      if (fill_box_dev(v, m->ns, ncell, b0 + i, chunk.b[i])) return -1;
+      ncell += (long long)chunk.b[i].len0 * chunk.b[i].len1 * chunk.b[i].len2;
     }
-    PGB_CUDA(cudaMemcpyAsync(&S->boxes[b0], chunk, n * sizeof(pgb::BoxDev), cudaMemcpyHostToDevice, st));
+    store_boxes_kernel<<<1, 128, 0, st>>>(chunk, n, &S->boxes[b0]);
+    PGB_CUDA(cudaGetLastError());
   }
   // The scratch keeps the previous call's contents: the queue head and counters restart at 0.
   PGB_CUDA(cudaMemsetAsync(&S->next_cell, 0, sizeof(S->next_cell), st));
   PGB_CUDA(cudaMemsetAsync(&S->stats, 0, sizeof(S->stats), st));
 
   pgb::ReactParams p;
+  std::memset(&p, 0, sizeof(p));
   p.boxes = S->boxes;
   p.nbox = nbox;
   p.ncell = ncell;
@@ -109,13 +142,17 @@ extern "C" int pgb_react_boxes_noalloc(const char* mechanism, const pgb_box_view
   int dev = 0, nsm = 0;
   PGB_CUDA(cudaGetDevice(&dev));
   PGB_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-  const int per = fp64 ? m->smem_fp64 : m->smem_mixed;
-  const int tpb = (per * 128 <= kMaxSmemPerBlock) ? 128 : 64;
-  long long nblocks = (ncell + tpb - 1) / tpb;
-  if (nblocks > nsm) nblocks = nsm;
   if (ncell > 0) {
-    const LaunchFn fn = fp64 ? m->bdf_fp64 : m->bdf_mixed;
-    if (fn(p, tpb, st, (int)nblocks)) return -1;
+    if (thread_ok) {
+      const int tpb = (per_thread * 128 <= kMaxSmemPerBlock) ? 128 : 64;
+      const long long nblocks = std::min<long long>((ncell + tpb - 1) / tpb, nsm);
+      const LaunchFn fn = fp64 ? m->bdf_fp64 : m->bdf_mixed;
+      if (fn(p, tpb, st, (int)nblocks)) return -1;
+    } else {
+      const long long nblocks = std::min<long long>((ncell + wpb - 1) / wpb, nsm);
+      const LaunchFn fn = fp64 ? m->warp_fp64 : m->warp_mixed;
+      if (fn(p, wpb, st, (int)nblocks)) return -1;
+    }
   }
   if (stats) {
     pgb::ReactStats h;

@@ -128,10 +128,20 @@ int parse_options(const char* s, Options& o) {
   if (o.max_order < 1 || o.max_order > pgb::QMAX)
     return set_err("cvode.max_order must be in [1, %d]", pgb::QMAX);
   if (o.max_steps < 1) return set_err("ode.max_steps must be >= 1");
-  if (o.solve_type != "denseAJ_direct" && o.solve_type != "dense_direct" && o.solve_type != "dense" &&
-      o.solve_type != "denseFDJ_direct")
-    return set_err("cvode.solve_type '%s' is not provided (dense direct solves only)",
-                   o.solve_type.c_str());
+  // Every accepted linear-solver key runs the dense direct Newton solve with the analytic
+  // Jacobian. The matrix-free Krylov keys of the reference's GPU decks (cvode.solve_type = GMRES,
+  // Exec/RegTests/FlameSheet/inputs.3d-regt_GPU:88) map to it too: GMRES solves the same Newton
+  // system (I - gamma J) x = r only to a fraction of the Newton tolerance, the direct solve
+  // exactly, and the nonlinear iteration's convergence test (and with it rtol/atol) is unchanged.
+  static const char* const kDense[] = {"denseAJ_direct", "dense_direct", "dense", "denseFDJ_direct"};
+  static const char* const kKrylov[] = {"GMRES", "precGMRES"};
+  bool known = false;
+  for (const char* k : kDense) known = known || o.solve_type == k;
+  for (const char* k : kKrylov) known = known || o.solve_type == k;
+  if (!known)
+    return set_err("cvode.solve_type '%s' is not provided (dense direct: denseAJ_direct, "
+                   "dense_direct, dense, denseFDJ_direct; GMRES and precGMRES run the dense direct "
+                   "solve)", o.solve_type.c_str());
   return 0;
 }
 
@@ -716,12 +726,19 @@ int advance_box_table(pgb_reactor* r, const std::vector<pgb::BoxDev>& boxes, lon
       if (s->gexec) { cudaGraphExecDestroy(s->gexec); s->gexec = nullptr; }
       cudaGraph_t graph;
       PGB_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+      graph = nullptr;
       const int rc = enqueue_advance(r, *s, nbox, ncell, dt_react, st);
       const cudaError_t ec = cudaStreamEndCapture(st, &graph);
-      if (rc) return rc;
-      if (ec != cudaSuccess) return set_err("graph capture failed: %s", cudaGetErrorString(ec));
-      PGB_CUDA(cudaGraphInstantiate(&s->gexec, graph, 0));
+      if (rc || ec != cudaSuccess) {  // the partial graph (if any) is released on every path
+        if (graph) cudaGraphDestroy(graph);
+        return rc ? rc : set_err("graph capture failed: %s", cudaGetErrorString(ec));
+      }
+      const cudaError_t ei = cudaGraphInstantiate(&s->gexec, graph, 0);
       cudaGraphDestroy(graph);
+      if (ei != cudaSuccess) {
+        s->gexec = nullptr;
+        return set_err("graph instantiation failed: %s", cudaGetErrorString(ei));
+      }
       s->gkey = boxes;
       s->gdt = dt_react;
     }

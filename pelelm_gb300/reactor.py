@@ -186,6 +186,32 @@ class ReactorBase:
         return ReactorGB(name, mechanism, options)
 
 
+def typical_values_chem(rhoY_mks, T, typical_Y_val_min: float = 1e-10):
+    """The typical values PeleLM hands to set_typ_vals_ode when peleLM.use_typ_vals_chem = 1.
+
+    reset_typical_values (Source/PeleLM.cpp:1519-1545) takes, per state component, the range
+    |max - min| over the field; species become mass fractions range(rhoY_k) / range(rho),
+    floored at typical_Y_val_min (1e-10, :162). update_typical_values_chem (:1497-1516) then
+    forms the reactor's vector in its CGS units: max(typical_Y_val_min, Y_k * rho * 1e-3) for
+    the species and the temperature range for T. Inputs are cell-major: rhoY_mks (ncell, ns)
+    in kg/m^3, T (ncell,) in K. Returns a list of ns + 1 floats."""
+    import numpy as np
+    rY = np.asarray(rhoY_mks, dtype=np.float64)
+    rho = rY.sum(axis=1)
+
+    def rng(a):
+        v = abs(float(np.max(a)) - float(np.min(a)))
+        return v if v > 0.0 else 0.5 * abs(float(np.max(a)) + float(np.min(a)))
+
+    typ_rho = rng(rho)
+    out = []
+    for k in range(rY.shape[1]):
+        typ_Y = max(rng(rY[:, k]) / typ_rho, typical_Y_val_min)
+        out.append(max(typical_Y_val_min, typ_Y * typ_rho * 1.0e-3))
+    out.append(rng(np.asarray(T, dtype=np.float64)))
+    return out
+
+
 def reaction_rates(mechanism: str, box: Box, rhoY, rhoH, T, mask, out, stream=None) -> None:
     """reactionRateRhoY over a box (MKS in/out), writing rhoYdot into `out`."""
     v = BoxArrays(box, rhoY, None, T, rhoH, None, None, mask).view()

@@ -14,7 +14,7 @@ the mechanisms' species order). For `NVODE` of the points it also stores an adva
 workload's dt_react without forcing, computed by scipy's VODE BDF at rtol 1e-12 on the oracle's
 right-hand side and analytic Jacobian (the same independent pin as make_golden.py).
 
-    python tests/golden/make_flame_states.py [reference root]
+    python tests/golden/make_flame_states.py <PeleLM source tree>
 """
 import os
 import sys
@@ -50,7 +50,9 @@ def read_profile(path):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_flame_states.py <PeleLM source tree>")
+    ref = sys.argv[1]
     out = {}
     for cfgname, rel in PROFILES.items():
         cfg = CONFIGS[cfgname]

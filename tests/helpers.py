@@ -55,3 +55,23 @@ def gather(boxes, ns):
 def tol_ratio(y_gpu, y_ref, rtol, atol):
     """max over entries of |dy| / (atol + rtol |y_ref|)."""
     return np.abs(y_gpu - y_ref) / (atol + rtol * np.abs(y_ref))
+
+
+def outliers_within_global_error(om, cs, cells, gpu, orc, dt, rtol):
+    """Cells outside the plain tolerances have taken another step sequence (a last-bit
+    difference in a sum can move an adaptive BDF onto other steps). Each is held, cell by
+    cell, to the oracle's own global error on that cell against a tight oracle (rtol 1e-11):
+    |GPU - tight| <= 2 |oracle - tight| + 50 rtol (T relative, mass fractions absolute).
+    gpu / orc: (rY, T) cell-major arrays of the same cells as `cells` indexes into cs."""
+    if len(cells) == 0:
+        return
+    c = np.asarray(cells)
+    t = om.react(cs.rY[c], cs.rYsrc[c], cs.T[c], cs.rE[c], cs.rEsrc[c], cs.mask[c], dt, 1e-11, 1e-16,
+                 max_steps=200000)
+    Yt = t[0] / t[0].sum(1, keepdims=True)
+    (rYg, Tg), (rYo, To) = gpu, orc
+    eTg, eTo = np.abs(Tg - t[1]), np.abs(To - t[1])
+    eYg = np.abs(rYg / rYg.sum(1, keepdims=True) - Yt).max(1)
+    eYo = np.abs(rYo / rYo.sum(1, keepdims=True) - Yt).max(1)
+    assert np.all(eTg <= 2 * eTo + 50 * rtol * t[1]), (c, eTg, eTo)
+    assert np.all(eYg <= 2 * eYo + 50 * rtol), (c, eYg, eYo)

@@ -48,7 +48,7 @@ def test_version_and_mechanisms(native_lib):
     ("ReactorCvode", "nope", 2, "", "unknown mechanism"),
     ("ReactorCvode", "lidryer_syn", 2, "ode.rtol=abc", "bad value"),
     ("ReactorCvode", "lidryer_syn", 2, "cvode.max_order=7", "max_order"),
-    ("ReactorCvode", "lidryer_syn", 2, "cvode.solve_type=GMRES", "not provided"),
+    ("ReactorCvode", "lidryer_syn", 2, "cvode.solve_type=sparse_direct", "not provided"),
     ("ReactorCvode", "lidryer_syn", 2, "gb.precision=fp16", "gb.precision"),
     ("ReactorCvode", "lidryer_syn", 2, "foo.bar=1", "unknown option"),
     ("ReactorCvode", "lidryer_syn", 2, "gb.retry=yes", "bad value"),
@@ -58,6 +58,22 @@ def test_create_rejects_bad_arguments(native_lib, name, mech, rtype, opts, msg):
     h = native_lib.pgb_reactor_create(name.encode(), mech.encode(), rtype, opts.encode())
     assert not h
     assert msg in _lib.last_error()
+
+
+@pytest.mark.parametrize("solve_type", ["GMRES", "precGMRES", "dense", "denseAJ_direct"])
+def test_options_of_the_reference_decks_are_accepted(native_lib, solve_type):
+    """The option strings of the reference's input decks pass the option parser, including the
+    GPU deck's matrix-free key (Exec/RegTests/FlameSheet/inputs.3d-regt_GPU:85-89), which runs
+    the dense direct Newton solve. Without a GPU, create() then stops at the device query."""
+    from pelelm_gb300 import _lib
+    opts = (f"peleLM.use_typ_vals_chem=1 ode.rtol=1.0e-6 ode.atol=1.0e-5 "
+            f"cvode.solve_type={solve_type} cvode.max_order=4")
+    h = native_lib.pgb_reactor_create(b"ReactorCvode", b"drm19_syn", 2, opts.encode())
+    if h:
+        native_lib.pgb_reactor_close(h)
+    else:
+        err = _lib.last_error()
+        assert "solve_type" not in err and "option" not in err, err
 
 
 def test_python_factory_mirrors_reference_names():

@@ -14,7 +14,7 @@ import os
 import numpy as np
 import pytest
 
-from helpers import boxes_from_cells, gather, tol_ratio
+from helpers import boxes_from_cells, gather, outliers_within_global_error, tol_ratio
 from pelelm_gb300.reactor import ReactorBase
 from pelelm_gb300.workloads import CONFIGS, make_cells, mech_path
 
@@ -43,7 +43,7 @@ def _run(torch, cfg, cs, sides, opts, **kw):
 
 CASES = [("lidryer_amr120", 2048, [8, 8, 8, 8], "gb.mapping=warp"),
          ("drm19_2M", 1024, [8, 8], "gb.mapping=warp"),
-         ("gri_1M", 256, [(8, 8, 4)], "")]
+         ("gri_1M", 2048, [(16, 16, 8)], "")]
 
 
 def _errs(tight, rY, T):
@@ -64,19 +64,32 @@ def test_warp_kernel_against_oracle(native_lib, oracle_mod, cuda, cfgname, n, si
     om = oracle_mod.OracleMech(mech_path(cfg.mech))
     rYo, To, rEo, FCo, nf = om.react(cs.rY, cs.rYsrc, cs.T, cs.rE, cs.rEsrc, cs.mask, cfg.dt, cfg.rtol, cfg.atol)
     tight = om.react(cs.rY, cs.rYsrc, cs.T, cs.rE, cs.rEsrc, cs.mask, cfg.dt, 1e-11, 1e-16, max_steps=200000)
-    relT = np.abs(Tg - To) / To
-    ratio = tol_ratio(rYg, rYo, cfg.rtol, cfg.atol).max(1)
+    # A few GRI-shaped cells per 10^4 fail in any FP64 BDF (Newton convergence failures; the
+    # oracle fails the same ones): cells the oracle fails may fail here too, no other cell may,
+    # and the comparisons run over the cells both sides integrate.
+    ok = (FCo > 0) & (FCg > 0)
+    assert np.all(FCg[FCo > 0] > 0), "a cell the oracle integrates failed on the GPU"
+    assert nf <= max(2, n // 1000)
+    relT = np.abs(Tg - To)[ok] / To[ok]
+    ratio = tol_ratio(rYg[ok], rYo[ok], cfg.rtol, cfg.atol).max(1)
     within = (relT <= 1e-6) & (ratio <= 1.0)
-    eg, eo = _errs(tight, rYg, Tg), _errs(tight, rYo, To)
+    tok = tight[3] > 0
+    sel = ok & tok
+    tsel = tuple(x[sel] if getattr(x, "ndim", 0) else x for x in tight)
+    eg, eo = _errs(tsel, rYg[sel], Tg[sel]), _errs(tsel, rYo[sel], To[sel])
     _report(f"warp[{cfgname},{precision}]", {
-        "frac_within_plain_tol": float(within.mean()), "max_relT": float(relT.max()),
-        "max_ratio": float(ratio.max()), "frac_same_nfe": float(np.mean(FCg == FCo)),
-        "nfe_gpu": float(FCg.mean()), "nfe_orc": float(FCo.mean()), "nfail": int(st["nfail"]),
+        "cells": int(n), "frac_within_plain_tol": float(within.mean()), "max_relT": float(relT.max()),
+        "max_ratio": float(ratio.max()), "frac_same_nfe": float(np.mean(FCg[ok] == FCo[ok])),
+        "nfe_gpu": float(FCg[ok].mean()), "nfe_orc": float(FCo[ok].mean()), "nfail": int(st["nfail"]),
+        "nfail_oracle": int(nf),
         "err_vs_tight_gpu": [float(x) for x in eg], "err_vs_tight_oracle": [float(x) for x in eo]})
-    assert st["nfail"] == 0 and nf == 0 and np.all(FCg > 0)
-    np.testing.assert_allclose(rEg, rEo, rtol=1e-14, atol=1e-14 * np.abs(rEo).max())
+    np.testing.assert_allclose(rEg[ok], rEo[ok], rtol=1e-14, atol=1e-14 * np.abs(rEo).max())
     if precision == "fp64":
         assert within.mean() >= 0.99, within.mean()
+        # every cell outside the plain tolerances is held, cell by cell, to the oracle's own
+        # global error on that cell against the tight oracle
+        out = np.nonzero(ok)[0][~within]
+        outliers_within_global_error(om, cs, out, (rYg[out], Tg[out]), (rYo[out], To[out]), cfg.dt, cfg.rtol)
     Tmax = float(np.max(tight[1]))
     bounds = ((2.0, 50 * cfg.rtol * Tmax), (1.25, 1e-3), (2.0, 50 * cfg.rtol), (1.25, 1e-8))
     for a, b, (fac, slack) in zip(eg, eo, bounds):
