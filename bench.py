@@ -3,15 +3,18 @@
 
 Default workload (one "step" = one advance of every cell of every box over dt_react):
   drm19-shaped CH4/air mechanism (21 species, 84 reactions; synthetic, structure-matched),
-  48 x 32^3 + 128 x 16^3 = 2^21 cells, T = 300 + 1900 c, phi ~ U[0.6, 1.4], dt_react = 1e-5 s,
-  rtol 1e-6, atol 1e-10, N(0, 1e2^2) kg/m^3/s species forcing (realizable, zero net mass) and
-  N(0, 1e8^2) W/m^3 energy forcing. Inputs are seeded synthetic states (no dataset exists).
-  The reactor runs the trained surrogate (pelelm_gb300/data/drm19_syn.pgbs) over every cell;
-  cells failing its checks, plus a 1% audit sample, are advanced by the GPU BDF in the same
-  CUDA graph. The same workload through the plain GPU BDF, the share of the step in each
-  kernel and the error of the result against the FP64 oracle at rtol 1e-10 (stratified
-  subsample) are reported beside it. --config lidryer_amr120 --surrogate none gives the plain
-  BDF on the 2,154,496-cell LiDryer-shaped AMR workload.
+  96 x 32^3 + 256 x 16^3 = 2^22 cells (the surrogate benchmark's inference size), T = 300 + 1900 c,
+  phi ~ U[0.6, 1.4], dt_react = 1e-5 s, rtol 1e-6, atol 1e-10, N(0, 1e2^2) kg/m^3/s species
+  forcing (realizable, zero net mass) and N(0, 1e8^2) W/m^3 energy forcing. Inputs are seeded
+  synthetic states (no dataset exists). The reactor runs the trained surrogate
+  (pelelm_gb300/data/drm19_syn.pgbs) over every cell; cells failing its checks, plus a 1% audit
+  sample, are advanced by the GPU BDF in the same CUDA graph. Reported beside it: the same
+  workload through the plain GPU BDF (mixed precision, and FP64 throughout), the share of the
+  step in each kernel, the error of the result against the FP64 oracle at rtol 1e-10
+  (stratified subsample), and compact lines (plain GPU BDF mixed and FP64 with their rooflines,
+  CPU oracle beside them) for the LiDryer 32^3 box, the LiDryer 120-box AMR workload and a
+  65,536-cell subset of the GRI-shaped workload. `--config lidryer_amr120 --surrogate none`
+  gives the plain BDF on the 2,154,496-cell LiDryer-shaped AMR workload as the headline.
 
 Arms:
   default            the GB300 reactor through its C ABI (pgb_reactor_react_boxes).
@@ -19,9 +22,9 @@ Arms:
                      all host cores, timed on a bounded sample of the same workload.
 
 Timing: W warm-up steps, then K timed steps, each bracketed by a barrier and
-torch.cuda.synchronize() with CUDA events on the launch stream; the device state (1.2 GB for
-drm19_2M) exceeds L2 (129 MB) and is restored from a pristine copy between steps (untimed).
-`e2e` repeats the steps from pinned host memory with the H2D input copies and D2H result
+torch.cuda.synchronize() with CUDA events on the launch stream; the device state (2.3 GB for
+drm19_4M) exceeds L2 (129 MB) and is restored from a pristine copy between steps (untimed).
+`e2e` repeats min(K, 3) steps from pinned host memory with the H2D input copies and D2H result
 copies inside the timed region.
 """
 from __future__ import annotations
@@ -49,7 +52,7 @@ def parse():
     p.add_argument("--steps", type=int, default=2)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb", choices=["gb", "reference"])
-    p.add_argument("--config", default="drm19_2M")
+    p.add_argument("--config", default="drm19_4M")
     p.add_argument("--surrogate", default="pelelm_gb300/data/drm19_syn.pgbs",
                    help="trained surrogate file, or 'none' for the plain GPU BDF")
     p.add_argument("--no-error-check", action="store_true")
@@ -57,6 +60,8 @@ def parse():
     p.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-fp64-line", action="store_true")
+    p.add_argument("--no-extras", action="store_true",
+                   help="skip the compact lines of the other benchmark configurations")
     p.add_argument("--cpu-sample", type=int, default=0,
                    help="cells timed on the CPU (0 = the whole workload, ~10 s on 16 cores)")
     p.add_argument("--profile-case", action="store_true",
@@ -160,17 +165,43 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------- workload
-def build_workload(cfg_name, seed):
-    from pelelm_gb300.workloads import CONFIGS, box_layout, make_cells, to_box_arena
-    cfg = CONFIGS[cfg_name]
-    cs = make_cells(cfg, seed=seed)
-    lay = box_layout(cfg.boxes)
-    arenas = {
-        "rY": to_box_arena(lay, cs.rY), "rY_src": to_box_arena(lay, cs.rYsrc),
-        "T": to_box_arena(lay, cs.T[:, None]), "rEner": to_box_arena(lay, cs.rE[:, None]),
-        "rEner_src": to_box_arena(lay, cs.rEsrc[:, None]),
-    }
-    return cfg, cs, lay, arenas
+class Shard:
+    """This rank's boxes of the global box list and their host arenas (component-major block per
+    box, boxes one after another).
+
+    The global list holds one copy of the configuration's boxes per rank (per-GPU work fixed as
+    ranks are added: weak scaling); global box g is a cube of side cfg.boxes[g % nbox] whose cells
+    are drawn from their own stream seeded (0, g), so any rank can build any box. Boxes go to
+    ranks by pelelm_gb300.sharding.partition_boxes over `weights` (cell counts before the first
+    advance, the boxes' FC sums after it)."""
+
+    def __init__(self, cfg, ws, rank, weights=None):
+        from pelelm_gb300.sharding import partition_boxes
+        from pelelm_gb300.workloads import box_layout, make_box_cells, to_box_arena
+        self.sides_global = list(cfg.boxes) * ws
+        w = (np.array([s ** 3 for s in self.sides_global], dtype=np.float64) if weights is None
+             else np.asarray(weights, dtype=np.float64))
+        self.ranks, self.load = partition_boxes(w, ws)
+        self.boxes = [g for g in range(len(self.sides_global)) if self.ranks[g] == rank]
+        self.cs = make_box_cells(cfg, self.sides_global, self.boxes, seed=0)
+        self.lay = box_layout([self.sides_global[g] for g in self.boxes])
+        cs = self.cs
+        self.arenas = {
+            "rY": to_box_arena(self.lay, cs.rY), "rY_src": to_box_arena(self.lay, cs.rYsrc),
+            "T": to_box_arena(self.lay, cs.T[:, None]), "rEner": to_box_arena(self.lay, cs.rE[:, None]),
+            "rEner_src": to_box_arena(self.lay, cs.rEsrc[:, None]),
+        }
+
+    @property
+    def ncell(self):
+        return self.lay.ncell
+
+    def fc_weights(self, fc):
+        """{global box: sum of its cells' FC} from the flat device FC array of this shard."""
+        from pelelm_gb300.sharding import fc_weights
+        off = self.lay.cell_offset
+        w = fc_weights([fc[int(off[i]):int(off[i + 1])] for i in range(len(self.boxes))])
+        return {g: float(x) for g, x in zip(self.boxes, w)}
 
 
 def box_views(torch, lay, dev, ns):
@@ -195,11 +226,13 @@ def run_gb(args, ws, rank, local, pg):
     from pelelm_gb300.reactor import ReactorBase
     from pelelm_gb300.workloads import load_mechanism
 
+    from pelelm_gb300.workloads import CONFIGS
     torch.cuda.set_device(local)
     dev_index = local
-    cfg, cs, lay, arenas = build_workload(args.config, seed=rank)
+    cfg = CONFIGS[args.config]
+    shard = Shard(cfg, ws, rank)
     mech = load_mechanism(cfg.mech)
-    ns, ncell = mech.ns, lay.ncell
+    ns = mech.ns
     surrogate = args.surrogate if args.surrogate != "none" else None
     if surrogate and not os.path.isabs(surrogate):
         surrogate = os.path.join(ROOT, surrogate)
@@ -212,10 +245,17 @@ def run_gb(args, ws, rank, local, pg):
 
     stream = torch.cuda.Stream()
     fields = ["rY", "rY_src", "T", "rEner", "rEner_src"]
-    pristine = {k: torch.from_numpy(arenas[k]).to("cuda") for k in fields}
-    work = {k: v.clone() for k, v in pristine.items()}
-    work["FC"] = torch.zeros(ncell, dtype=torch.float64, device="cuda")
-    views = box_views(torch, lay, work, ns)
+    pristine, work, views = {}, {}, []
+
+    def upload():
+        pristine.clear()
+        work.clear()
+        pristine.update({k: torch.from_numpy(shard.arenas[k]).to("cuda") for k in fields})
+        work.update({k: v.clone() for k, v in pristine.items()})
+        work["FC"] = torch.zeros(shard.ncell, dtype=torch.float64, device="cuda")
+        views[:] = box_views(torch, shard.lay, work, ns)
+
+    upload()
     base_opts = f"ode.rtol={cfg.rtol} ode.atol={cfg.atol} gb.graph=1 gb.autotune=1"
 
     def make_reactor(precision, extra=""):
@@ -254,7 +294,30 @@ def run_gb(args, ws, rank, local, pg):
 
     sg_opts = f"gb.surrogate={surrogate}" if surrogate else ""
     r = make_reactor(args.precision, sg_opts)
-    t_step, clocks, st = timed_steps(r, args.steps, args.warmup)
+    rebalance = None
+    if ws > 1:
+        # the first warm-up advance runs the cell-count partition; every rank then shares its
+        # boxes' FC sums (host objects, between advances) and all ranks re-partition the global
+        # box list by that cost, as PeleLM's getFuncCountDM does with the previous FuncCount
+        restore()
+        with torch.cuda.stream(stream):
+            r.react_boxes(views, cfg.dt, 0.0, stream=stream)
+        torch.cuda.synchronize()
+        mine = shard.fc_weights(work["FC"])
+        allw = [None] * ws
+        pg.all_gather_object(allw, mine)
+        weights = np.zeros(len(shard.sides_global))
+        for d in allw:
+            for g, x in d.items():
+                weights[int(g)] = x
+        load_cells = shard.load
+        shard = Shard(cfg, ws, rank, weights)
+        upload()
+        rebalance = {"by": "FC sums of the first warm-up advance", "boxes_global": len(shard.sides_global),
+                     "max_over_mean_load": float(shard.load.max() / max(shard.load.mean(), 1e-300)),
+                     "cell_partition_max_over_mean_cells": float(load_cells.max() / max(load_cells.mean(), 1e-300))}
+    t_step, clocks, st = timed_steps(r, args.steps, max(args.warmup - (1 if ws > 1 else 0), 1))
+    ncell, cs, lay, arenas = shard.ncell, shard.cs, shard.lay, shard.arenas
     sst = r.surrogate_stats() if surrogate else None
     tuning = r.tuning()
     t_max = allmax(pg, t_step)
@@ -270,7 +333,8 @@ def run_gb(args, ws, rank, local, pg):
     h2d = sum(v.numel() * 8 for v in host_in.values())
     d2h = sum(v.numel() * 8 for v in host_out.values())
     e2e_total = 0.0
-    for i in range(1 + args.steps):
+    n_e2e = max(1, min(args.steps, 3))  # cells/s is size- and step-independent at this scale
+    for i in range(1 + n_e2e):
         torch.cuda.synchronize()
         barrier(pg, dev_index)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -287,7 +351,7 @@ def run_gb(args, ws, rank, local, pg):
         barrier(pg, dev_index)
         if i >= 1:
             e2e_total += e0.elapsed_time(e1) / 1e3
-    e2e_value = allsum(pg, float(ncell * args.steps)) / allmax(pg, e2e_total)
+    e2e_value = allsum(pg, float(ncell * n_e2e)) / allmax(pg, e2e_total)
     r.close()
 
     flops_rhs = rhs_flops(mech)
@@ -340,16 +404,24 @@ def run_gb(args, ws, rank, local, pg):
         nfe = st["nfe"]
         achieved = flops_rhs * nfe / (t_step / args.steps) / 1e12
         dominant = "bdf_reactor_kernel"
-        if not args.no_fp64_line and args.precision != "fp64":
-            r64 = make_reactor("fp64")
-            t64, _, st64 = timed_steps(r64, max(1, min(args.steps, 2)), 1, clocks=False)
-            extra["fp64_plain"] = {"cells_per_s": ncell * max(1, min(args.steps, 2)) / t64,
-                                   "ms_per_step": 1e3 * t64 / max(1, min(args.steps, 2)),
-                                   "nfe_per_step": st64["nfe"]}
-            r64.close()
+    if not args.no_fp64_line and args.precision != "fp64":
+        # the plain GPU BDF in FP64 throughout (the reference's own precision) on the same
+        # workload: the like-for-like figure beside the mixed-precision one
+        n64 = 1
+        r64 = make_reactor("fp64")
+        t64, _, st64 = timed_steps(r64, n64, 1, clocks=False)
+        r64.close()
+        extra["fp64_plain_gpu_bdf"] = {
+            "cells_per_s": allsum(pg, float(ncell * n64)) / allmax(pg, t64), "ms_per_step": 1e3 * t64 / n64,
+            "steps": n64, "warmup": 1, "nfe_per_cell": st64["nfe"] / ncell, "nfail": int(st64["nfail"]),
+            "roofline_frac": flops_rhs * st64["nfe"] / (t64 / n64) / 1e12 / fp64_peak}
 
     if rank == 0 and cfg.mech != "gri_syn":
         extra["rate_evaluation"] = rates_roofline(torch, cfg, cs, stream, flops_rhs, fp64_peak)
+    if rank == 0 and not args.no_extras:
+        others = EXTRA_CONFIGS + ([] if args.config.startswith("drm19") else [("drm19_2M", None)])
+        extra["other_configs"] = {name: config_extra(torch, name, ncells, stream, fp64_peak, cpu=not args.no_cpu_baseline)
+                                  for name, ncells in others if name != args.config}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -366,13 +438,19 @@ def run_gb(args, ws, rank, local, pg):
                        (" | learned surrogate (4x256 GELU BF16 MLP ensemble, fused inference) with "
                         "BDF fallback and 1% audit" if surrogate else " | plain GPU BDF"),
                        "precision": args.precision, "cells_per_gpu": ncell,
+                       "sharding": ("one global box list (one copy of the configuration's boxes per "
+                                    "rank), partitioned by pgb_partition_boxes: cell counts for the first "
+                                    "warm-up advance, then the boxes' FC sums" if ws > 1 else
+                                    "single rank: every box"),
+                       **({"rebalance": rebalance} if rebalance else {}),
                        "l2": f"inputs ({ncell * (3 * ns + 5) * 8 / 1e6:.0f} MB of state) larger than L2; "
                              "state restored between steps",
                        "launch": "surrogate kernel -> persistent work-stealing BDF on the device fallback "
                                  "list -> audit kernel, one CUDA graph per step" if surrogate else
                                  "one persistent work-stealing kernel per step, CUDA-graph replay",
                        "autotune": tuning},
-            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "steps": n_e2e, "warmup": 1},
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
                          "frac": achieved / fp64_peak,
                          # DRAM bytes per launch from an ncu capture of a smaller launch of the same
@@ -395,6 +473,73 @@ def run_gb(args, ws, rank, local, pg):
         if cpu:
             line["cpu_baseline"] = cpu
         print(json.dumps(line), flush=True)
+
+
+# Compact lines for the other benchmark configurations: (config, cells; None = all). The
+# GRI-shaped line runs a stated 65,536-cell subset of gri_1M (its BDF takes ~40 s per 2^20 cells).
+# The drm19 2^21-cell plain configuration is the headline's plain_gpu_bdf leg (same state
+# distribution on 2^22 cells), so it gets its own line only when the headline runs elsewhere.
+EXTRA_CONFIGS = [("lidryer_32cube", None), ("lidryer_amr120", None), ("gri_1M", 65536)]
+
+
+def config_extra(torch, name, ncells, stream, fp64_peak, cpu=True, steps=1, warm=1):
+    """Plain GPU BDF on one benchmark configuration (mixed and FP64, CUDA events on the launch
+    stream, state restored between steps), its FP64 rate-evaluation roofline and, on a bounded
+    sample, the CPU oracle beside it."""
+    from pelelm_gb300.mech.opcount import rhs_flops
+    from pelelm_gb300.reactor import BoxArrays, ReactorBase
+    from pelelm_gb300.workloads import CONFIGS, box_layout, load_mechanism, make_cells, to_box_arena
+    cfg = CONFIGS[name]
+    mech = load_mechanism(cfg.mech)
+    ns = mech.ns
+    if ncells is None:
+        sides = list(cfg.boxes)
+        cs = make_cells(cfg, seed=0)
+    else:
+        sides = [16] * (ncells // 4096)
+        cs = make_cells(cfg, 4096 * len(sides), seed=0)
+    lay = box_layout(sides)
+    n = lay.ncell
+    host = {"rY": cs.rY, "rY_src": cs.rYsrc, "T": cs.T[:, None], "rEner": cs.rE[:, None],
+            "rEner_src": cs.rEsrc[:, None]}
+    pristine = {k: torch.from_numpy(to_box_arena(lay, a)).to("cuda") for k, a in host.items()}
+    work = {k: v.clone() for k, v in pristine.items()}
+    work["FC"] = torch.zeros(n, dtype=torch.float64, device="cuda")
+    views = box_views(torch, lay, work, ns)
+    flops = rhs_flops(mech)
+    out = {"workload": WORKLOAD_TEXT.get(name, name) + (f" | {n}-cell subset in 16^3 boxes" if ncells else ""),
+           "cells": n}
+    for precision in ("mixed", "fp64"):
+        r = ReactorBase.create("ReactorCvode", cfg.mech, f"ode.rtol={cfg.rtol} ode.atol={cfg.atol} gb.graph=1 "
+                               f"gb.precision={precision}")
+        r.init(2, 1)
+        t = 0.0
+        for i in range(warm + steps):
+            for k in pristine:
+                work[k].copy_(pristine[k])
+            work["FC"].zero_()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(stream):
+                e0.record(stream)
+                r.react_boxes(views, cfg.dt, 0.0, stream=stream)
+                e1.record(stream)
+            torch.cuda.synchronize()
+            if i >= warm:
+                t += e0.elapsed_time(e1) / 1e3
+        st = r.stats()
+        r.close()
+        out[precision] = {"cells_per_s": n * steps / t, "ms_per_step": 1e3 * t / steps, "steps": steps,
+                          "warmup": warm, "nfe_per_cell": st["nfe"] / n, "nst_per_cell": st["nst"] / n,
+                          "nfail": int(st["nfail"]), "nretry": int(st["nretry"]),
+                          "roofline": {"bound": "fp64", "unit": "TFLOP/s",
+                                       "achieved": flops * st["nfe"] / (t / steps) / 1e12, "peak": fp64_peak,
+                                       "frac": flops * st["nfe"] / (t / steps) / 1e12 / fp64_peak,
+                                       "what": f"{flops} FP64 flops per RHS x RHS evaluations / BDF time"}}
+    if cpu:
+        res = cpu_baseline(cfg, cs, min(n, default_cpu_sample(cfg) // 4), single_core=False)
+        out["cpu_oracle"] = {k: res[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    return out
 
 
 def rates_roofline(torch, cfg, cs, stream, flops_rhs, fp64_peak, reps=5):
@@ -538,9 +683,9 @@ def cpu_baseline(cfg, cs, sample, nthreads=0, single_core=True):
 def run_reference(args, ws, rank, pg):
     if rank != 0:
         return
-    from pelelm_gb300.workloads import CONFIGS, make_cells
+    from pelelm_gb300.workloads import CONFIGS
     cfg = CONFIGS[args.config]
-    cs = make_cells(cfg, seed=0)
+    cs = Shard(cfg, 1, 0).cs  # the GB300 arm's single-rank workload
     # each step: a bounded sample (a few seconds on 16 cores), so K + W steps stay in minutes
     sample = args.cpu_sample or default_cpu_sample(cfg) // 4
     vals = []

@@ -211,6 +211,25 @@ int pgb_react_boxes_noalloc(const char* mechanism, const pgb_box_view* views, in
                             double dt_react, double rtol, double atol, int max_order, int max_steps,
                             int fp64, void* stream, pgb_stats* stats);
 
+/* ---- Work partition across ranks (one rank per GPU); host-only, no device call. ----
+ * The analogue of PeleLM's chemistry load balance on CPU builds: chop the grids until there are
+ * enough boxes per rank (Source/PeleLM.cpp:5699-5723), then a knapsack over each box's summed
+ * FuncCount of the previous advance (getFuncCountDM, Source/PeleLM.cpp:5530-5623). The cells are
+ * independent, so each rank advances its boxes with no communication. */
+
+/* Halves the longest side of the largest box (ties: first) while the list holds fewer than
+ * `target` boxes and a box has a side of at least 2 * min_side; each piece keeps its parent's
+ * index in parent[] (the caller's arrays still cover it). out/parent hold `cap` entries.
+ * Returns the number of boxes written, or -1. */
+int pgb_chop_boxes(const pgb_box* in, int nin, int min_side, int target, pgb_box* out, int* parent, int cap);
+
+/* Assigns box b (weight[b] >= 0: its FC sum, or its cell count before the first advance) to
+ * rank_of_box[b] in [0, nranks): heaviest first to the least loaded rank, then moves and swaps
+ * between the most and least loaded ranks while the largest load strictly drops. Deterministic.
+ * load (optional, nranks entries) receives each rank's total. The largest load is at most the
+ * mean load plus the largest weight. Returns 0, or -1. */
+int pgb_partition_boxes(const double* weight, int nbox, int nranks, int* rank_of_box, double* load);
+
 /* ---- Learned surrogate: BF16 tensor-core building blocks (FP32 accumulation). No counterpart in
  * the reference: they train and evaluate the MLP that predicts a cell's (dY, dT) over dt_react.
  * All pointers are device memory; bf16 arrays are passed as void*. ---- */

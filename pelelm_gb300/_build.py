@@ -21,7 +21,7 @@ BUILD = os.path.join(PKG, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-std=c++17", "-O3", "-lineinfo", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
            "-Xcompiler", "-O2"]
-UNITS = ["reactor.cu", "peak.cu", "noalloc.cu", "mlp.cu", "surrogate_io.cu", "mech_lidryer_syn.cu", "mech_drm19_syn.cu",
+UNITS = ["reactor.cu", "peak.cu", "noalloc.cu", "partition.cpp", "mlp.cu", "surrogate_io.cu", "mech_lidryer_syn.cu", "mech_drm19_syn.cu",
          "mech_gri_syn.cu"]
 
 
@@ -53,7 +53,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     generate_sources()
     deps = [os.path.join(dp, f) for dp, _, fs in os.walk(CSRC) for f in fs
-            if f.endswith((".cu", ".cuh", ".h"))]
+            if f.endswith((".cu", ".cuh", ".h", ".cpp"))]
     deps.append(os.path.join(ROOT, "include", "pelelm_gb300.h"))
     if not force and not _sources_newer(LIB, deps):
         return LIB
@@ -61,7 +61,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
 
     def compile_unit(u):
         src = os.path.join(CSRC, u)
-        obj = os.path.join(BUILD, u.replace(".cu", ".o"))
+        obj = os.path.join(BUILD, os.path.splitext(u)[0] + ".o")
         cmd = [nvcc(), *NVFLAGS, *ARCH, "-c", src, "-o", obj]
         if verbose:
             cmd.insert(1, "-Xptxas=-v")

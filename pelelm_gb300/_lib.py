@@ -67,6 +67,8 @@ EXPORTS = {
     "pgb_reaction_rates": (C.c_int, [C.c_char_p, C.POINTER(BoxView), C.POINTER(Array4), _vp]),
     "pgb_rhoh_to_temp": (C.c_int, [C.c_char_p, C.POINTER(BoxView), C.c_double, C.c_double, _vp]),
     "pgb_fp64_peak_tflops": (C.c_int, [C.c_int, C.POINTER(C.c_double)]),
+    "pgb_chop_boxes": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _vp, _vp, C.c_int]),
+    "pgb_partition_boxes": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp]),
     "pgb_mlp_gemm_nt": (C.c_int, [_vp, C.c_int, _vp, C.c_int, C.c_int, C.c_int, C.c_int, _vp, C.c_int,
                                   _vp, _vp, _vp, C.c_int, C.c_int, _vp]),
     "pgb_mlp_transpose_bf16": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _vp, C.c_int, _vp]),

@@ -14,6 +14,7 @@ component).
 """
 from __future__ import annotations
 
+import functools
 import os
 from dataclasses import dataclass, field
 from typing import Dict, List, Optional
@@ -25,8 +26,13 @@ from .mech.model import Mechanism, R_ERG, P_ATM
 DATA_DIR = os.path.join(os.path.dirname(__file__), "data")
 
 
-def load_mechanism(name: str) -> Mechanism:
+@functools.lru_cache(maxsize=None)
+def _load_mechanism_cached(name: str) -> Mechanism:
     return Mechanism.from_json(os.path.join(DATA_DIR, f"{name}.json"))
+
+
+def load_mechanism(name: str) -> Mechanism:
+    return _load_mechanism_cached(name)
 
 
 def mech_path(name: str, ext: str = "mech") -> str:
@@ -214,6 +220,16 @@ def make_cells(cfg: Config, ncell: Optional[int] = None, seed: int = 0) -> CellS
         rEsrc = rng.normal(0.0, cfg.sigma_h_mks, n) * 10.0  # W/m^3 -> erg/cm^3/s
     mask = np.ones(n, dtype=np.int32)
     return CellState(rY=rY, rYsrc=rYsrc, T=T, rE=rE, rEsrc=rEsrc, mask=mask, p=p)
+
+
+def make_box_cells(cfg: Config, sides: List[int], box_ids, seed: int = 0) -> CellState:
+    """Cells of the cubic boxes `box_ids` of a box list with sides `sides` (cells of one box in
+    i-fastest order, boxes in the order given). Box b draws from its own stream, seeded
+    (seed, b), so any subset of a box list, on any rank, gets the same cells as the whole."""
+    parts = [make_cells(cfg, int(sides[b]) ** 3, seed=[int(seed), int(b)]) for b in box_ids]
+    if not parts:
+        return make_cells(cfg, 0, seed=seed)
+    return CellState(**{k: np.concatenate([getattr(p, k) for p in parts]) for k in CellState.__annotations__})
 
 
 @dataclass
