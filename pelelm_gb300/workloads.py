@@ -14,6 +14,7 @@ component).
 """
 from __future__ import annotations
 
+import copy
 import functools
 import os
 from dataclasses import dataclass, field
@@ -32,7 +33,8 @@ def _load_mechanism_cached(name: str) -> Mechanism:
 
 
 def load_mechanism(name: str) -> Mechanism:
-    return _load_mechanism_cached(name)
+    """The named mechanism (a private copy: callers may modify it)."""
+    return copy.deepcopy(_load_mechanism_cached(name))
 
 
 def mech_path(name: str, ext: str = "mech") -> str:
@@ -187,7 +189,7 @@ class CellState:
 
 
 def make_cells(cfg: Config, ncell: Optional[int] = None, seed: int = 0) -> CellState:
-    mech = load_mechanism(cfg.mech)
+    mech = _load_mechanism_cached(cfg.mech)  # read only
     n = cfg.ncell if ncell is None else int(ncell)
     rng = np.random.default_rng(seed)
     phi = rng.uniform(cfg.phi[0], cfg.phi[1], n)
