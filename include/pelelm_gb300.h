@@ -67,7 +67,8 @@ typedef struct {
  * Jacobian; the GPU decks' matrix-free GMRES / precGMRES keys run that same Newton solve
  * directly), ode.analytical_jacobian,
  * peleLM.use_typ_vals_chem, plus ode.max_steps, gb.precision=fp64|mixed, gb.tpb, gb.graph=0|1,
- * gb.history=shared|global, gb.lu=shared|global, gb.mapping=thread|warp, gb.wpb, gb.autotune=0|1
+ * gb.history=shared|global, gb.lu=shared|global, gb.mapping=thread|warp|group (one cell per
+ * thread, per warp, or per group of gb.group = 4|8 lanes), gb.wpb, gb.autotune=0|1
  * (time every compiled mapping on the first advance's cells, keep the fastest), gb.retry=0|1
  * (default 1: cells the mixed-precision pass fails are integrated again from their inputs by
  * the FP64 kernel in the same call), and

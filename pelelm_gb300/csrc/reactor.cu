@@ -58,7 +58,8 @@ struct Options {
   bool graph = false;
   int z_global = -1;       // gb.history = shared | global (L2-resident Nordsieck); -1 = auto
   int lu_global = -1;      // gb.lu = shared | global (L2-resident Jacobian/LU); -1 = auto
-  int mapping = -1;        // gb.mapping = thread (cell per thread) | warp (cell per warp); -1 = auto
+  int mapping = -1;        // gb.mapping = thread | warp | group (cell per thread / warp / lane group); -1 = auto
+  int group = 8;           // gb.group: lanes per cell of the group mapping (4 or 8)
   int wpb = 0;             // gb.wpb: warps per block of the warp mapping (0 = most that fit)
   bool autotune = false;   // gb.autotune: time the compiled mappings on the first advance's cells
   bool retry = true;       // gb.retry: cells the mixed-precision pass fails are integrated again in FP64
@@ -97,7 +98,11 @@ int parse_options(const char* s, Options& o) {
       else if (k == "gb.mapping") {
         if (v == "thread") o.mapping = 0;
         else if (v == "warp") o.mapping = 1;
-        else return set_err("gb.mapping must be thread or warp, got '%s'", v.c_str());
+        else if (v == "group") o.mapping = 2;
+        else return set_err("gb.mapping must be thread, warp or group, got '%s'", v.c_str());
+      } else if (k == "gb.group") {
+        o.group = std::stoi(v);
+        if (o.group != 4 && o.group != 8) return set_err("gb.group must be 4 or 8, got '%s'", v.c_str());
       } else if (k == "gb.wpb") o.wpb = std::stoi(v);
       else if (k == "gb.autotune") o.autotune = std::stoi(v) != 0;
       else if (k == "gb.retry") o.retry = std::stoi(v) != 0;
@@ -290,10 +295,11 @@ struct LaunchPlan {
   int tpb = 128, nblocks = 1;
   bool z_global = false, lu_global = false;
   size_t z_bytes = 0, lu_bytes = 0;
-  bool warp = false;  // warp-per-cell kernel; tpb then holds warps per block
+  bool warp = false;   // warp-per-cell kernel; tpb then holds warps per block
+  bool group = false;  // group-per-cell kernel; tpb then holds lanes per cell
 };
 
-bool use_warp(const pgb_reactor* r);
+int mapping_of(const pgb_reactor* r);
 
 // First layout (all shared; global Nordsieck history; global history and LU) whose shared
 // footprint fits 128 threads per block (the occupancy that measures best), unless options
@@ -303,7 +309,16 @@ bool use_warp(const pgb_reactor* r);
 LaunchPlan plan_launch(const pgb_reactor* r, long long ncell, bool mixed) {
   LaunchPlan pl;
   const MechEntry& m = *r->mech;
-  if (use_warp(r)) {
+  if (mapping_of(r) == 2) {
+    // lane groups per cell: as many warps per block as fit shared memory, one block per SM
+    const int G = r->opt.group;
+    const int per_block = (mixed ? m.group_cells_mixed : m.group_cells_fp64)(G);
+    pl.group = true;
+    pl.tpb = G;
+    pl.nblocks = (int)std::min<long long>(r->nsm, std::max<long long>(1, (ncell + per_block - 1) / std::max(per_block, 1)));
+    return pl;
+  }
+  if (mapping_of(r) == 1) {
     // warp per cell: as many warps per block as fit shared memory (or gb.wpb), one block per SM
     const int per = mixed ? m.wsmem_mixed : m.wsmem_fp64;
     int wpb = r->opt.wpb;
@@ -357,14 +372,17 @@ int ensure_buf(Scratch& s, void*& buf, size_t& cap, size_t bytes) {
   return 0;
 }
 
-// Cell-per-thread kernels exist for mechanisms whose per-cell state fits a thread; gb.mapping
-// overrides the default below.
-bool use_warp(const pgb_reactor* r) {
-  if (!r->mech->bdf_mixed) return true;
-  if (r->opt.mapping >= 0) return r->opt.mapping == 1;
-  // measured: cell per thread for the 9-species mechanism (4x faster), cell per warp from the
-  // 21-species one on (1.8x faster: the per-thread state no longer fits registers)
-  return r->mech->ns > 12;
+// Kernel mapping: 0 cell per thread, 1 cell per warp, 2 cell per lane group. Cell-per-thread
+// kernels exist for mechanisms whose per-cell state fits a thread, group kernels for the
+// 21-species size; gb.mapping overrides the default below.
+int mapping_of(const pgb_reactor* r) {
+  if (r->opt.mapping >= 0) return r->opt.mapping;
+  if (!r->mech->bdf_mixed) return 1;
+  // measured: cell per thread for the 9-species mechanism (4x faster than per warp); from the
+  // 21-species one on the per-thread state no longer fits registers: lane groups where compiled,
+  // else one warp per cell
+  if (r->mech->ns <= 12) return 0;
+  return r->mech->group_mixed ? 2 : 1;
 }
 
 // Audit records kept per call: twice the expected sample plus slack (cells past the capacity
@@ -401,8 +419,9 @@ int enqueue_advance(pgb_reactor* r, Scratch& s, int nbox, long long ncell, doubl
   const LaunchPlan pl = plan_launch(r, ncell, r->opt.mixed);
   p.lu_scratch = pl.lu_bytes ? s.d_lu : nullptr;
   p.z_scratch = pl.z_bytes ? s.d_z : nullptr;
-  LaunchFn fn = pl.warp ? (r->opt.mixed ? r->mech->warp_mixed : r->mech->warp_fp64)
-                        : (r->opt.mixed ? r->mech->bdf_mixed : r->mech->bdf_fp64);
+  LaunchFn fn = pl.group ? (r->opt.mixed ? r->mech->group_mixed : r->mech->group_fp64)
+               : pl.warp ? (r->opt.mixed ? r->mech->warp_mixed : r->mech->warp_fp64)
+                         : (r->opt.mixed ? r->mech->bdf_mixed : r->mech->bdf_fp64);
   // mixed precision with retry: the cells its pass fails (FP32 Newton matrices can stall where
   // FP64 ones converge) are listed on the device and integrated again from their untouched
   // inputs by the FP64 kernel, on the same stream (and in the same graph)
@@ -425,7 +444,7 @@ int enqueue_advance(pgb_reactor* r, Scratch& s, int nbox, long long ncell, doubl
     q.lu_scratch = p64.lu_bytes ? s.d_lu : nullptr;
     q.z_scratch = p64.z_bytes ? s.d_z : nullptr;
     PGB_CUDA(cudaMemsetAsync(s.d_counter, 0, sizeof(unsigned long long), st));
-    const LaunchFn f64 = p64.warp ? r->mech->warp_fp64 : r->mech->bdf_fp64;
+    const LaunchFn f64 = p64.group ? r->mech->group_fp64 : p64.warp ? r->mech->warp_fp64 : r->mech->bdf_fp64;
     return f64(q, p64.tpb, st, p64.nblocks);
   };
   if (!r->sg.d_net) return run_bdf();
@@ -506,6 +525,10 @@ pgb_reactor* pgb_reactor_create(const char* name, const char* mechanism, int rea
   if (parse_options(options, o)) return nullptr;
   if (o.mapping == 0 && !m->bdf_mixed) {
     set_err("mechanism '%s' has no cell-per-thread kernel (gb.mapping=warp)", m->name);
+    return nullptr;
+  }
+  if (o.mapping == 2 && !m->group_mixed) {
+    set_err("mechanism '%s' has no group-per-cell kernel (gb.mapping=warp)", m->name);
     return nullptr;
   }
   if (!o.surrogate.empty() && !m->sg_fn) {
@@ -603,12 +626,15 @@ int run_autotune(pgb_reactor* r, const std::vector<pgb::BoxDev>& boxes, long lon
   const long long nsample = std::min<long long>(ncell, 32768);
   const long long stride = std::max<long long>(1, ncell / nsample);
   const size_t arena_bytes = (size_t)nf * nsample * sizeof(double);
-  struct Cand { int mapping, wpb; };
+  struct Cand { int mapping, wpb; };  // wpb: warps per block (warp mapping), lanes per cell (group)
   std::vector<Cand> cands;
   if (m.bdf_mixed) cands.push_back({0, 0});
   const int per = r->opt.mixed ? m.wsmem_mixed : m.wsmem_fp64;
   for (int i = 0; i < 4 && m.wpb_choice[i] > 0; ++i)
     if (m.wpb_choice[i] * per <= kMaxSmemPerBlock) cands.push_back({1, m.wpb_choice[i]});
+  if (m.group_mixed)
+    for (int G : {8, 4})
+      if ((r->opt.mixed ? m.group_cells_mixed : m.group_cells_fp64)(G) > 0) cands.push_back({2, G});
   if (cands.size() < 2) {
     r->tuning = "single compiled mapping: nothing to tune";
     return 0;
@@ -654,9 +680,13 @@ int run_autotune(pgb_reactor* r, const std::vector<pgb::BoxDev>& boxes, long lon
     std::ostringstream rep;
     double best = 1e300;
     Cand pick = cands[0];
+    auto name = [](const Cand& c) {
+      return c.mapping == 0 ? std::string("thread")
+                            : (c.mapping == 1 ? "warp/" : "group/") + std::to_string(c.wpb);
+    };
     for (const Cand& c : cands) {
       r->opt.mapping = c.mapping;
-      r->opt.wpb = c.wpb;
+      if (c.mapping == 2) r->opt.group = c.wpb; else r->opt.wpb = c.wpb;
       const LaunchPlan pl = plan_launch(r, nsample, r->opt.mixed);
       if (ensure_buf(sc, sc.d_z, sc.z_cap, pl.z_bytes) || ensure_buf(sc, sc.d_lu, sc.lu_cap, pl.lu_bytes)) { rc = -1; break; }
       float ms = 0.f;
@@ -669,8 +699,7 @@ int run_autotune(pgb_reactor* r, const std::vector<pgb::BoxDev>& boxes, long lon
         cudaEventElapsedTime(&ms, e0, e1);
       }
       if (rc) break;
-      rep << (c.mapping ? "warp/" : "thread") << (c.mapping ? std::to_string(c.wpb) : std::string()) << " " << ms
-          << " ms; ";
+      rep << name(c) << " " << ms << " ms; ";
       if (ms < best) { best = ms; pick = c; }
     }
     cudaEventDestroy(e0);
@@ -678,8 +707,8 @@ int run_autotune(pgb_reactor* r, const std::vector<pgb::BoxDev>& boxes, long lon
     if (rc) break;
     r->opt = saved;
     r->opt.mapping = pick.mapping;
-    r->opt.wpb = pick.wpb;
-    rep << "on " << nsample << " sample cells -> " << (pick.mapping ? "warp/" + std::to_string(pick.wpb) : std::string("thread"));
+    if (pick.mapping == 2) r->opt.group = pick.wpb; else r->opt.wpb = pick.wpb;
+    rep << "on " << nsample << " sample cells -> " << name(pick);
     r->tuning = rep.str();
   } while (false);
   if (rc) r->opt = saved;

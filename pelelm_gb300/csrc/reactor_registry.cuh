@@ -9,6 +9,7 @@
 #include <cstring>
 
 #include "../../include/pelelm_gb300.h"
+#include "bdf_group_kernel.cuh"
 #include "bdf_kernel.cuh"
 #include "bdf_warp_kernel.cuh"
 #include "point_kernels.cuh"
@@ -120,6 +121,47 @@ int launch_bdf_warp(const pgb::ReactParams& p, int wpb, cudaStream_t s, int nblo
   return set_err("warp BDF: %d warps per block are not compiled for %s", wpb, M::NAME);
 }
 
+// Group-per-cell BDF: G lanes per cell, as many warps per block as fit shared memory (at most
+// 16), one persistent block per SM.
+template <class M, class JR, int G>
+constexpr int group_wpb() {
+  constexpr int per = pgb::gbdf_smem_per_warp<M, JR, G>();
+  constexpr int w = kMaxSmemPerBlock / per;
+  return w > 16 ? 16 : w;
+}
+
+template <class M, class JR, int G>
+int launch_bdf_group_g(const pgb::ReactParams& p, cudaStream_t s, int nblocks) {
+  constexpr int WPB = group_wpb<M, JR, G>();
+  if constexpr (WPB < 1) {
+    return set_err("group BDF: one warp of %d-lane groups needs %d B of shared memory (limit %d)", G,
+                   pgb::gbdf_smem_per_warp<M, JR, G>(), kMaxSmemPerBlock);
+  } else {
+    constexpr int smem = WPB * pgb::gbdf_smem_per_warp<M, JR, G>();
+    auto kern = pgb::bdf_group_kernel<M, JR, G, WPB>;
+    PGB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    kern<<<nblocks, WPB * 32, smem, s>>>(p);
+    PGB_CUDA(cudaGetLastError());
+    return 0;
+  }
+}
+
+// Cells one block of the group kernel holds (warps per block x cells per warp).
+template <class M, class JR>
+int group_cells_per_block(int G) {
+  if (G == 8) return group_wpb<M, JR, 8>() * 4;
+  if (G == 4) return group_wpb<M, JR, 4>() * 8;
+  return 0;
+}
+
+// The group size is the launch argument (LaunchFn's second parameter).
+template <class M, class JR>
+int launch_bdf_group(const pgb::ReactParams& p, int G, cudaStream_t s, int nblocks) {
+  if (G == 8) return launch_bdf_group_g<M, JR, 8>(p, s, nblocks);
+  if (G == 4) return launch_bdf_group_g<M, JR, 4>(p, s, nblocks);
+  return set_err("group BDF: %d lanes per cell are not compiled (4, 8)", G);
+}
+
 template <class M>
 int launch_null(const pgb::ReactParams& p, cudaStream_t s, int nblocks) {
   pgb::null_reactor_kernel<M><<<nblocks, 256, 0, s>>>(p);
@@ -170,6 +212,8 @@ struct MechEntry {
   int (*sg_feat_fn)(const pgb::BoxDev*, int, long long, float*, cudaStream_t);
   int wpb_choice[4];  // warps per block compiled for the warp kernel, preferred first, 0-ended
   int (*hr_fn)(const pgb_box*, const pgb_array4*, const pgb_array4*, const pgb_array4*, cudaStream_t);
+  LaunchFn group_mixed, group_fp64;  // group-per-cell BDF (argument: lanes per cell, 4 or 8)
+  int (*group_cells_mixed)(int), (*group_cells_fp64)(int);  // cells per block for a group size
 };
 
 
@@ -270,7 +314,31 @@ int h2t_entry(const pgb_box_view* v, double tmin, double tmax, cudaStream_t s) {
       ::pgb_host::warp_wpb_choice<M>(0), ::pgb_host::warp_wpb_choice<M>(1),                  \
           ::pgb_host::warp_wpb_choice<M>(2), ::pgb_host::warp_wpb_choice<M>(3)               \
     }                                                                                        \
-    , ::pgb_host::heat_release_entry<M>                                                      \
+    , ::pgb_host::heat_release_entry<M>, nullptr, nullptr, nullptr, nullptr                 \
+  }
+
+// Mechanisms whose cells also run group-per-cell (the 21-species size): all of the above plus
+// the group kernel in both precisions.
+#define PGB_MECH_ENTRY_GROUP(M)                                                              \
+  ::pgb_host::MechEntry {                                                                    \
+    M::NAME, M::NS, M::NR, ::pgb_host::launch_bdf<M, float>, ::pgb_host::launch_bdf<M, double>, \
+        ::pgb_host::launch_null<M>, pgb::bdf_smem_per_thread<M, float>(),                    \
+        pgb::bdf_smem_per_thread<M, double>(),                                               \
+        pgb::bdf_smem_per_thread<M, float, pgb::LAYOUT_Z_GLOBAL>(),                          \
+        pgb::bdf_smem_per_thread<M, double, pgb::LAYOUT_Z_GLOBAL>(),                         \
+        pgb::bdf_smem_per_thread<M, float, 3>(), pgb::bdf_smem_per_thread<M, double, 3>(),   \
+        ::pgb_host::rates_entry<M>,                                                          \
+        ::pgb_host::h2t_entry<M>, ::pgb_host::launch_surrogate<M>,                           \
+        ::pgb_host::launch_surrogate_audit<M>, ::pgb_host::launch_bdf_warp<M, float>,        \
+        ::pgb_host::launch_bdf_warp<M, double>, pgb::bdf_warp_smem_per_warp<M, float>(),     \
+        pgb::bdf_warp_smem_per_warp<M, double>(), ::pgb_host::launch_surrogate_features<M>,  \
+    {                                                                                        \
+      ::pgb_host::warp_wpb_choice<M>(0), ::pgb_host::warp_wpb_choice<M>(1),                  \
+          ::pgb_host::warp_wpb_choice<M>(2), ::pgb_host::warp_wpb_choice<M>(3)               \
+    }                                                                                        \
+    , ::pgb_host::heat_release_entry<M>, ::pgb_host::launch_bdf_group<M, float>,             \
+        ::pgb_host::launch_bdf_group<M, double>, ::pgb_host::group_cells_per_block<M, float>, \
+        ::pgb_host::group_cells_per_block<M, double>                                         \
   }
 
 // Mechanisms too large for one cell per thread: warp-per-cell BDF, ReactorNull and T(h, Y) only.
@@ -285,7 +353,7 @@ int h2t_entry(const pgb_box_view* v, double tmin, double tmax, cudaStream_t s) {
       ::pgb_host::warp_wpb_choice<M>(0), ::pgb_host::warp_wpb_choice<M>(1),                  \
           ::pgb_host::warp_wpb_choice<M>(2), ::pgb_host::warp_wpb_choice<M>(3)               \
     }                                                                                        \
-    , ::pgb_host::heat_release_entry<M>                                                      \
+    , ::pgb_host::heat_release_entry<M>, nullptr, nullptr, nullptr, nullptr                 \
   }
 
 // Converts and validates one box view into its device descriptor; cell numbering of the box

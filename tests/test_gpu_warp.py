@@ -1,5 +1,7 @@
 """GPU parity of the warp-per-cell BDF kernel (gb.mapping=warp; the only mapping compiled for
-the GRI-shaped mechanism, 53 species / 325 reactions) against the CPU oracle, through the C ABI.
+the GRI-shaped mechanism, 53 species / 325 reactions) and of the lane-group kernel
+(gb.mapping=group, 4 or 8 lanes per cell; the drm19-shaped default) against the CPU oracle,
+through the C ABI.
 
 The warp kernel sums production rates, norms and the energy closure in a different order than
 the oracle (lanes, shuffles), so a cell can take a different step sequence; FP64 mode is held
@@ -43,6 +45,8 @@ def _run(torch, cfg, cs, sides, opts, **kw):
 
 CASES = [("lidryer_amr120", 2048, [8, 8, 8, 8], "gb.mapping=warp"),
          ("drm19_2M", 1024, [8, 8], "gb.mapping=warp"),
+         ("drm19_2M", 8192, [16, 16], "gb.mapping=group gb.group=8"),
+         ("drm19_2M", 4096, [16], "gb.mapping=group gb.group=4"),
          ("gri_1M", 2048, [(16, 16, 8)], "")]
 
 
@@ -131,13 +135,14 @@ def test_warp_kernel_boxes_ghosts_mask_graph(native_lib, oracle_mod, cuda):
 
 
 @pytest.mark.gpu
-def test_warp_kernel_is_deterministic_and_serves_the_surrogate_fallback(native_lib, cuda):
+@pytest.mark.parametrize("mapping", ["warp", "group"])
+def test_warp_kernel_is_deterministic_and_serves_the_surrogate_fallback(native_lib, cuda, mapping):
     """Two runs give identical bits (no atomics in the arithmetic); the surrogate's fallback
-    cells through the warp kernel equal the plain warp-kernel run bit for bit."""
+    cells through the warp (or lane-group) kernel equal the plain run bit for bit."""
     torch = cuda
     cfg = CONFIGS["drm19_2M"]
     cs = make_cells(cfg, 4096, seed=31)
-    base = "gb.mapping=warp gb.precision=mixed"
+    base = f"gb.mapping={mapping} gb.precision=mixed"
     (a, _), (b, _) = (_run(torch, cfg, cs, [16], base) for _ in range(2))
     for x, y in zip(a, b):
         assert np.array_equal(x, y)
@@ -178,8 +183,12 @@ def test_autotuner_picks_a_compiled_mapping_and_leaves_inputs_alone(native_lib, 
     r.close()
     _report(f"autotune[{cfgname}]", {"report": rep})
     assert "->" in rep and "thread" in rep and "warp/" in rep
+    if cfgname.startswith("drm19"):
+        assert "group/8" in rep and "group/4" in rep
     picked = rep.split("->")[-1].strip()
-    explicit = "gb.mapping=thread" if picked == "thread" else f"gb.mapping=warp gb.wpb={picked.split('/')[1]}"
+    kind, _, size = picked.partition("/")
+    explicit = {"thread": "gb.mapping=thread", "warp": f"gb.mapping=warp gb.wpb={size}",
+                "group": f"gb.mapping=group gb.group={size}"}[kind]
     (b, _) = _run(torch, cfg, cs, [16] * 4, "gb.precision=mixed " + explicit)
     for x, y in zip(a, b):
         assert np.array_equal(x, y)
@@ -202,7 +211,8 @@ def _run_graph_twice(torch, cfg, cs, sides, opts):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("cfgname,mapping", [("lidryer_amr120", "thread"), ("drm19_2M", "warp")])
+@pytest.mark.parametrize("cfgname,mapping", [("lidryer_amr120", "thread"), ("drm19_2M", "warp"),
+                                             ("drm19_2M", "group")])
 def test_mixed_precision_retries_failed_cells_in_fp64(native_lib, cuda, cfgname, mapping):
     """gb.retry (on by default in mixed precision): a cell the mixed-precision pass fails is
     integrated again, from its untouched inputs, by the FP64 kernel in the same call (and the
