@@ -87,7 +87,17 @@ def _cpW_expr(s, lo_flag, scale):
     return f"fma(T, fma(T, fma(T, fma(T, {c(4)}, {c(3)}), {c(2)}), {c(1)}), {c(0)})"
 
 
+def check_supported(m: Mechanism) -> None:
+    """The kernels take every reverse rate from K_c; explicit reverse Arrhenius parameters
+    (CHEMKIN REV, which the reader keeps) are refused here rather than silently ignored."""
+    for j, r in enumerate(m.reactions):
+        if r.rev is not None:
+            raise ValueError(f"{m.name}: reaction {j} ({r.equation()}) has explicit reverse parameters "
+                             "(REV), which the rate kernels do not evaluate")
+
+
 def gen_header(m: Mechanism) -> str:
+    check_supported(m)
     ns, nr = m.ns, m.nr
     N = ns + 1
     W = [s.W for s in m.species]
@@ -470,6 +480,7 @@ def gen_tables(m: Mechanism, space: str = "constant") -> str:
     the only choice when the tables exceed the 64 KB constant bank), plus the species-major list
     of the reactions each species takes part in with its net coefficient (production rates as a
     gather)."""
+    check_supported(m)
     glob = space == "global"
     qual = "__device__ const" if glob else "__device__ __constant__"
     nsname = f"tabg_{m.name}" if glob else f"tab_{m.name}"

@@ -19,7 +19,7 @@ R_CAL = 1.98720425864083  # cal/mol/K
 R_ERG = 8.31446261815324e7  # erg/mol/K
 P_ATM = 1.01325e6  # dyn/cm^2
 
-ATOMIC_WEIGHT = {"H": 1.008, "C": 12.011, "N": 14.007, "O": 15.999, "Ar": 39.95}
+ATOMIC_WEIGHT = {"H": 1.008, "C": 12.011, "N": 14.007, "O": 15.999, "Ar": 39.95, "He": 4.0026}
 
 
 @dataclass
@@ -49,6 +49,8 @@ class Reaction:
     low: Optional[Arrhenius] = None      # k_0 (falloff)
     troe: Optional[List[float]] = None   # [alpha, T3, T1] or [alpha, T3, T1, T2]; None => Lindemann
     efficiencies: Dict[str, float] = field(default_factory=dict)  # third-body (default 1)
+    rev: Optional[Arrhenius] = None      # explicit reverse Arrhenius (CHEMKIN REV); None => K_c
+    duplicate: bool = False              # CHEMKIN DUPLICATE marker (no kinetic effect)
 
     def equation(self) -> str:
         def side(d):
@@ -98,6 +100,8 @@ class Mechanism:
             r["rate"] = Arrhenius(**r["rate"])
             if r.get("low") is not None:
                 r["low"] = Arrhenius(**r["low"])
+            if r.get("rev") is not None:
+                r["rev"] = Arrhenius(**r["rev"])
             rx.append(Reaction(**r))
         return Mechanism(name=d["name"], elements=d["elements"], species=sp, reactions=rx,
                          synthetic=d.get("synthetic", True), seed=d.get("seed", 0),
@@ -114,6 +118,10 @@ class Mechanism:
         """
         el_idx = {e: i for i, e in enumerate(self.elements)}
         kinds = {"elementary": 0, "three_body": 1, "falloff": 2}
+        for j, r in enumerate(self.reactions):
+            if r.rev is not None:
+                raise ValueError(f"reaction {j} ({r.equation()}): explicit reverse Arrhenius parameters "
+                                 "(REV) are not supported by the rate kernels; reverse rates come from K_c")
         out = [f"{self.ns} {self.nr} {len(self.elements)}"]
         for s in self.species:
             comp = " ".join(f"{el_idx[e]} {n}" for e, n in s.composition.items())
