@@ -60,6 +60,8 @@ def parse():
     p.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-fp64-line", action="store_true")
+    p.add_argument("--no-pareto", action="store_true",
+                   help="skip the surrogate's looser operating points (acceptance vs tolerance)")
     p.add_argument("--no-extras", action="store_true",
                    help="skip the compact lines of the other benchmark configurations")
     p.add_argument("--cpu-sample", type=int, default=0,
@@ -399,6 +401,10 @@ def run_gb(args, ws, rank, local, pg):
         }
         if rank == 0 and not args.no_error_check:
             extra["error_vs_fp64_oracle"] = error_vs_oracle(cfg, cs, lay, out_state, args.error_sample)
+        if not args.no_pareto:
+            extra["surrogate_pareto"] = surrogate_pareto(
+                surrogate, make_reactor, sg_opts, timed_steps, work, plain_cps, ncell, pg, rank, cfg, cs, lay,
+                args.error_sample, None if args.no_error_check else error_vs_oracle)
         dominant = "bdf_reactor_kernel (fallback cells)"
     else:
         nfe = st["nfe"]
@@ -473,6 +479,34 @@ def run_gb(args, ws, rank, local, pg):
         if cpu:
             line["cpu_baseline"] = cpu
         print(json.dumps(line), flush=True)
+
+
+def surrogate_pareto(surrogate, make_reactor, sg_opts, timed_steps, work, plain_cps, ncell, pg, rank, cfg, cs,
+                     lay, sample, error_fn):
+    """The surrogate at each calibrated operating point of its sidecar file (<file>.levels.json:
+    1 K / 1e-4, 2 K / 3e-4, 5 K / 1e-3, 10 K / 3e-3): one warm-up and one timed advance of the
+    whole workload each, the accepted fraction, the speed-up over the plain GPU BDF and the error
+    of the accepted cells against the FP64 oracle at rtol 1e-10 (stratified subsample)."""
+    with open(surrogate + ".levels.json") as f:
+        levels = json.load(f)["levels"]
+    out = []
+    for lv in levels:
+        opts = sg_opts + " " + " ".join(f"gb.sg.{k}={lv[k]!r}" for k in ("mis", "cons", "disT", "disY", "neg",
+                                                                           "tol_T", "tol_Y"))
+        r = make_reactor("mixed", opts)
+        t, _, _ = timed_steps(r, 1, 1, clocks=False)
+        sst = r.surrogate_stats()
+        r.close()
+        cps = allsum(pg, float(ncell)) / allmax(pg, t)
+        pt = {"tol_T_K": lv["tol_T"], "tol_Y": lv["tol_Y"], "accepted_frac": sst["accept"] / max(sst["ncell"], 1),
+              "cells_per_s": cps, "speedup_vs_plain_gpu_bdf": cps / plain_cps,
+              "calibration_accepted_frac": lv.get("val_accept")}
+        if error_fn is not None and rank == 0 and sst["accept"] > 0:
+            e = error_fn(cfg, cs, lay, {k: work[k].clone() for k in ("rY", "T", "FC")}, sample)["surrogate_cells"]
+            pt["accepted_cells_vs_oracle"] = e
+            pt["within_tolerance"] = bool(e["max_dT_K"] <= lv["tol_T"] and e["max_dY"] <= lv["tol_Y"])
+        out.append(pt)
+    return out
 
 
 # Compact lines for the other benchmark configurations: (config, cells; None = all). The
