@@ -21,8 +21,29 @@ BUILD = os.path.join(PKG, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-std=c++17", "-O3", "-lineinfo", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
            "-Xcompiler", "-O2"]
-UNITS = ["reactor.cu", "peak.cu", "noalloc.cu", "partition.cpp", "mlp.cu", "surrogate_io.cu", "mech_lidryer_syn.cu", "mech_drm19_syn.cu",
-         "mech_gri_syn.cu"]
+# host and shared units; each mechanism adds a generated csrc/gen/unit_<name>.cu
+UNITS = ["reactor.cu", "peak.cu", "noalloc.cu", "partition.cpp", "mlp.cu", "surrogate_io.cu"]
+DATA = os.path.join(PKG, "data")
+
+
+def mechanism_names() -> list:
+    """Every mechanism description in pelelm_gb300/data (<name>.json holding species and
+    reactions): the three built-in synthetic ones first, then others (e.g. converted from
+    CHEMKIN input by pelelm_gb300.mech.chemkin) in name order."""
+    import json
+    names = []
+    for f in sorted(os.listdir(DATA)):
+        if not f.endswith(".json") or f.count(".") != 1:
+            continue
+        try:
+            with open(os.path.join(DATA, f)) as fh:
+                d = json.load(fh)
+        except (OSError, ValueError):
+            continue
+        if isinstance(d, dict) and "species" in d and "reactions" in d:
+            names.append(f[:-5])
+    first = [n for n in ("lidryer_syn", "drm19_syn", "gri_syn") if n in names]
+    return first + [n for n in names if n not in first]
 
 
 def nvcc() -> str:
@@ -32,14 +53,24 @@ def nvcc() -> str:
     return p
 
 
-def generate_sources() -> None:
+def generate_sources() -> list:
+    """Mechanism headers, tables, per-mechanism units and the registry list; returns the
+    generated unit paths. The oracle's flat file is written for a mechanism that lacks one."""
     from .mech import codegen
+    from .workloads import load_mechanism
     gen = os.path.join(CSRC, "gen")
-    codegen.main(gen, names=("lidryer_syn", "drm19_syn", "gri_syn"))
-    codegen.write_tables(gen, names=("lidryer_syn", "drm19_syn", "gri_syn"))
+    names = mechanism_names()
+    codegen.main(gen, names=names)
+    codegen.write_tables(gen, names=names)
+    units = codegen.write_units(gen, names)
+    for n in names:
+        flat = os.path.join(DATA, f"{n}.mech")
+        if not os.path.exists(flat):
+            load_mechanism(n).to_flat(flat)
     # the exp64 constants are committed (their generator needs mpmath, absent on some hosts)
     if not os.path.exists(os.path.join(gen, "exp64_table.cuh")):
         subprocess.check_call([sys.executable, os.path.join(CSRC, "gen_exp64.py")])
+    return units
 
 
 def _sources_newer(target: str, deps) -> bool:
@@ -51,16 +82,16 @@ def _sources_newer(target: str, deps) -> bool:
 
 def build(verbose: bool = False, force: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
-    generate_sources()
+    units = [os.path.join(CSRC, u) for u in UNITS] + generate_sources()
     deps = [os.path.join(dp, f) for dp, _, fs in os.walk(CSRC) for f in fs
-            if f.endswith((".cu", ".cuh", ".h", ".cpp"))]
+            if f.endswith((".cu", ".cuh", ".h", ".cpp", ".inc"))]
     deps.append(os.path.join(ROOT, "include", "pelelm_gb300.h"))
     if not force and not _sources_newer(LIB, deps):
         return LIB
     objs = []
 
-    def compile_unit(u):
-        src = os.path.join(CSRC, u)
+    def compile_unit(src):
+        u = os.path.basename(src)
         obj = os.path.join(BUILD, os.path.splitext(u)[0] + ".o")
         cmd = [nvcc(), *NVFLAGS, *ARCH, "-c", src, "-o", obj]
         if verbose:
@@ -70,8 +101,10 @@ def build(verbose: bool = False, force: bool = False) -> str:
             raise RuntimeError(f"nvcc failed for {u}:\n{r.stderr}")
         return obj, r.stderr
 
-    with cf.ThreadPoolExecutor(max_workers=max(1, min(len(UNITS), os.cpu_count() or 1))) as ex:
-        for obj, log in ex.map(compile_unit, UNITS):
+    # the largest units first, so the longest compile starts at once
+    units.sort(key=lambda p: -os.path.getsize(p) if os.path.basename(p).startswith("unit_") else 0)
+    with cf.ThreadPoolExecutor(max_workers=max(1, min(len(units), os.cpu_count() or 1))) as ex:
+        for obj, log in ex.map(compile_unit, units):
             objs.append(obj)
             if verbose and log:
                 print(log)

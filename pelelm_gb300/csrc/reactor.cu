@@ -36,11 +36,9 @@ int set_err(const char* fmt, ...) {
   return -1;
 }
 
-extern const MechEntry kEntry_lidryer_syn;
-extern const MechEntry kEntry_drm19_syn;
-extern const MechEntry kEntry_gri_syn;
-
 }  // namespace pgb_host
+
+#include "gen/mech_registry.inc"
 
 using namespace pgb_host;
 
@@ -980,7 +978,7 @@ int pgb_rhoh_to_temp(const char* mechanism, const pgb_box_view* view, double tmi
 
 namespace {
 
-const MechEntry* const kMechs[] = {&kEntry_lidryer_syn, &kEntry_drm19_syn, &kEntry_gri_syn};
+const MechEntry* const kMechs[] = {PGB_MECH_LIST};
 
 const MechEntry* find_mech(const char* name) {
   if (!name) return nullptr;

@@ -110,7 +110,7 @@ def gen_header(m: Mechanism) -> str:
     e(f"#ifndef {guard}")
     e(f"#define {guard}")
     e('#include "../mech_common.cuh"')
-    const_tab = m.name in CONSTANT_TABLES
+    const_tab = constant_tables(m)
     if const_tab:
         e(f'#include "tab_{m.name}.cuh"')
     e(f'#include "tabg_{m.name}.cuh"')
@@ -607,9 +607,20 @@ def gen_tables(m: Mechanism, space: str = "constant") -> str:
     return e.text()
 
 
-# mechanisms whose tables fit the 64 KB constant bank (per-thread kernels); every mechanism
-# also gets the global-memory tables of the warp-per-cell kernel
-CONSTANT_TABLES = ("lidryer_syn", "drm19_syn")
+def kernel_family(m: Mechanism) -> str:
+    """Which persistent BDF kernels a mechanism gets: "thread" (cell per thread and per warp)
+    up to 12 species, "group" (cell per thread, per lane group and per warp) while the ODE size
+    stays within one warp's lanes (N <= 32), else "warp" only (one cell's state no longer fits a
+    thread)."""
+    if m.ns <= 12:
+        return "thread"
+    return "group" if m.ns + 1 <= 32 else "warp"
+
+
+def constant_tables(m: Mechanism) -> bool:
+    """Tables in the 64 KB constant bank for the per-thread kernels (mechanisms that have them);
+    every mechanism also gets the global-memory tables of the lane-group and warp kernels."""
+    return kernel_family(m) != "warp"
 
 
 def write_tables(outdir: str, names=("lidryer_syn", "drm19_syn", "gri_syn")):
@@ -617,7 +628,7 @@ def write_tables(outdir: str, names=("lidryer_syn", "drm19_syn", "gri_syn")):
     for n in names:
         m = load_mechanism(n)
         outs = [(f"tabg_{n}.cuh", gen_tables(m, "global"))]
-        if n in CONSTANT_TABLES:
+        if constant_tables(m):
             outs.append((f"tab_{n}.cuh", gen_tables(m, "constant")))
         for fname, text in outs:
             path = os.path.join(outdir, fname)
@@ -627,3 +638,48 @@ def write_tables(outdir: str, names=("lidryer_syn", "drm19_syn", "gri_syn")):
                         continue
             with open(path, "w") as f:
                 f.write(text)
+
+
+# ---------------------------------------------------------------------------- registry
+_ENTRY_MACRO = {"thread": "PGB_MECH_ENTRY", "group": "PGB_MECH_ENTRY_GROUP", "warp": "PGB_MECH_ENTRY_WARP"}
+
+
+def write_units(outdir: str, names) -> list:
+    """One translation unit per mechanism (its kernels and registry entry) and the registry list
+    included by csrc/reactor.cu; returns the unit paths. Files are rewritten only on change."""
+    from ..workloads import load_mechanism
+
+    def put(path, text):
+        if os.path.exists(path):
+            with open(path) as f:
+                if f.read() == text:
+                    return
+        with open(path, "w") as f:
+            f.write(text)
+
+    units = []
+    reg = ["// GENERATED by pelelm_gb300/mech/codegen.py from the mechanisms in pelelm_gb300/data/.",
+           "// Registry of the compiled mechanisms (one unit_<name>.cu each), included by reactor.cu.",
+           "namespace pgb_host {"]
+    for n in names:
+        m = load_mechanism(n)
+        fam = kernel_family(m)
+        text = "\n".join([
+            f"// GENERATED by pelelm_gb300/mech/codegen.py from pelelm_gb300/data/{n}.json.",
+            f"// Kernels of mechanism {n} ({m.ns} species, {m.nr} reactions; BDF kernel family: {fam}) and",
+            "// its registry entry.",
+            f'#include "mech_{n}.cuh"',
+            '#include "../reactor_registry.cuh"',
+            "",
+            "namespace pgb_host {",
+            f"extern const MechEntry kEntry_{n} = {_ENTRY_MACRO[fam]}(pgb::Mech_{n});",
+            "}  // namespace pgb_host",
+            ""])
+        path = os.path.join(outdir, f"unit_{n}.cu")
+        put(path, text)
+        units.append(path)
+        reg.append(f"extern const MechEntry kEntry_{n};")
+    reg.append("}  // namespace pgb_host")
+    reg.append("#define PGB_MECH_LIST " + ", ".join(f"&::pgb_host::kEntry_{n}" for n in names))
+    put(os.path.join(outdir, "mech_registry.inc"), "\n".join(reg) + "\n")
+    return units

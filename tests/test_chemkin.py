@@ -161,3 +161,36 @@ def test_parser_errors(tmp_path, edit, msg):
     assert chem != CHEM
     with pytest.raises(ChemkinError, match=msg):
         read_chemkin(*_write_inputs(tmp_path, chem), name="bad")
+
+
+def test_converted_mechanism_compiles_as_a_library_unit(tmp_path):
+    """A mechanism read from CHEMKIN input becomes a library entry with no source edit: the
+    build generates its kernel header, tables, unit and registry line from the JSON. Here the
+    9-species mechanism, written out and read back under a new name, goes through the same
+    generators and its unit compiles for sm_103a (nvcc cross-compiles on a host without GPU)."""
+    import os
+    import shutil
+    import subprocess
+    from pelelm_gb300 import _build
+    from pelelm_gb300.mech import codegen
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(nvcc):
+        pytest.skip("nvcc not available")
+    m = load_mechanism("lidryer_syn")
+    write_chemkin(m, str(tmp_path / "chem.inp"), str(tmp_path / "therm.dat"))
+    r = read_chemkin(str(tmp_path / "chem.inp"), str(tmp_path / "therm.dat"), name="lidryer_ck")
+    gen = tmp_path / "gen"
+    gen.mkdir()
+    (gen / "mech_lidryer_ck.cuh").write_text(codegen.gen_header(r))
+    (gen / "tab_lidryer_ck.cuh").write_text(codegen.gen_tables(r, "constant"))
+    (gen / "tabg_lidryer_ck.cuh").write_text(codegen.gen_tables(r, "global"))
+    unit = gen / "unit_lidryer_ck.cu"
+    unit.write_text(f'#include "mech_lidryer_ck.cuh"\n#include "../reactor_registry.cuh"\n'
+                    "namespace pgb_host {\n"
+                    f"extern const MechEntry kEntry_lidryer_ck = PGB_MECH_ENTRY(pgb::Mech_lidryer_ck);\n}}\n")
+    assert codegen.kernel_family(r) == "thread"
+    csrc_gen = os.path.join(_build.CSRC, "gen")
+    cmd = [nvcc, *_build.NVFLAGS, *_build.ARCH, "-I", csrc_gen, "-c", str(unit), "-o", str(tmp_path / "u.o")]
+    res = subprocess.run(cmd, capture_output=True, text=True, timeout=600)
+    assert res.returncode == 0, res.stderr[-2000:]
+    assert "lidryer_ck" in subprocess.run(["nm", "-C", str(tmp_path / "u.o")], capture_output=True, text=True).stdout
