@@ -308,38 +308,40 @@ __device__ __noinline__ bool warp_setup(const WVec<M> yv, const double gamma, co
     Qw = warp_sum(Qw);
     cpw = warp_sum(cpw);
     __syncwarp();
-    // (2) assembly: lane owns species k = lane + 32 c and walks, in reaction order, only the
-    // reactions whose terms land in column k (k reacts, or a third body) — adding into column k
-    // and, where k is a slot species, into row k of the T column. Every matrix entry receives
-    // its additions in reaction order, then slot order, whatever the lane schedule.
+    // (2) assembly by the generated contribution program: each lane owns whole entries A[i][k]
+    // (species rows; k = NS: the T column) and sums their terms in a register, in the order of
+    // the reaction walk (reactions ascending, then row slots): a term of reaction j is
+    // +-(W_i / W_k) v with v the partials of j that land in column k, and +-W_i dq/dT in the T
+    // column. Each entry has one writer, so the result does not depend on the lane schedule.
+    {
+      const int e1 = Tab::jac_lane(lane + 1);
+#pragma unroll 1
+      for (int en = Tab::jac_lane(lane); en < e1; ++en) {
+        const int tg = Tab::jac_t(en);
+        const int i = tg / LDA, k = tg - i * LDA;
+        const JR wi = Tab::template sp<JR>(i).W;
+        const JR w = (k == NS) ? wi : wi * Tab::template sp<JR>(k).invW;
+        JR acc = JR(0);
+        const int c1 = Tab::jac_off(en + 1);
+#pragma unroll 1
+        for (int c = Tab::jac_off(en); c < c1; ++c) {
+          const int code = Tab::jac_code(c);
+          const JR* pj = RX + (code & 0xffff) * wbdf::RXW;
+          JR v;
+          if (code & (1 << 16)) {
+            v = pj[0];
+          } else {
+            v = JR(0);
 #pragma unroll
-    for (int cc = 0; cc < R; ++cc) {
-      const int k = idx(cc);
-      if (k >= NS) continue;
-      const JR iwk = Tab::template sp<JR>(k).invW;
-      const int e1 = Tab::col_end(k);
-#pragma unroll 1
-      for (int e = Tab::col_begin(k); e < e1; ++e) {
-        const int j = Tab::col_j(e);
-        const TabReaction<JR>& r = Tab::template rx<JR>(j);
-        const JR* pj = RX + j * wbdf::RXW;
-        JR v = JR(0);
-        for (int s = 0; s < r.nr; ++s) if (r.rs[s] == k) v += pj[1 + s];
-        for (int s = 0; s < r.np; ++s) if (r.ps[s] == k) v += pj[4 + s];
-        if (r.kind != 0) {
-          JR eff = JR(1);
-          const TabThirdBody<JR>& t = Tab::template tb<JR>(r.tb);
-          for (int q = 0; q < t.n; ++q) if (t.sp[q] == k) eff += t.effm1[q];
-          v += pj[7] * eff;
+            for (int q = 0; q < 6; ++q)
+              if (code & (1 << (17 + q))) v += pj[1 + q];
+            if (code & (1 << 23)) v += pj[7] * Tab::template jac_eff<JR>(c);
+            if (v == JR(0)) continue;
+          }
+          const JR cw = (code & (1 << 24)) ? -w : w;
+          acc += cw * v;
         }
-#pragma unroll 1
-        for (int row = 0; row < r.nr + r.np; ++row) {
-          const bool isr = row < r.nr;
-          const int i = isr ? r.rs[row] : r.ps[row - r.nr];
-          const JR sgnW = (isr ? JR(-1) : JR(1)) * Tab::template sp<JR>(i).W;
-          if (i == k) A[k * LDA + NS] += sgnW * pj[0];
-          if (v != JR(0)) A[i * LDA + k] += sgnW * iwk * v;
-        }
+        A[tg] = acc;
       }
     }
     __syncwarp();

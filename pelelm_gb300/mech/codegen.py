@@ -570,17 +570,62 @@ def gen_tables(m: Mechanism, space: str = "constant") -> str:
                     jj.append(j)
                     nu.append(float(net))
             off.append(len(jj))
-        # per species: the reactions whose Jacobian terms land in its column (it is a reactant or
-        # product, or the reaction has a third body: every species is a collider), in order
-        coff, cj = [0], []
-        for k in range(ns):
-            for j, (_, _, _, kind_, _, rs_, ps_, _, _, _) in enumerate(rx):
-                if k in rs_ or k in ps_ or kind_ != 0:
-                    cj.append(j)
-            coff.append(len(cj))
-        e(f"constexpr int NCOL = {len(cj)};")
-        e(f"{qual} int kColOff[NS + 1] = {{{', '.join(str(x) for x in coff)}}};")
-        e(f"{qual} int kColJ[NCOL] = {{{', '.join(str(x) for x in cj)}}};")
+        # Jacobian contribution program of the cooperative setup (warp and lane-group kernels):
+        # every nonzero species entry A[i][k] (and T-column entry A[i][NS]) of the analytic
+        # Jacobian with its ordered terms. A term of reaction j adds sign * w * v to the entry,
+        # w = W_i / W_k (W_i for the T column) and v the sum of reaction j's stored partials its
+        # code selects: bit 16 dq/dT (T column), bits 17-19 / 20-22 the reactant / product slots
+        # holding species k, bit 23 the collider term dq/d[M] times the efficiency of k; bit 24 a
+        # reactant row (negative sign); bits 0-15 the reaction. Terms keep the order of the
+        # column walk they replace: reactions ascending, then the row slots of the reaction.
+        # Entries go to the 32 lanes largest first, to the lane with the fewest terms so far.
+        N = ns + 1
+        LDA = N + 1
+        tbeff = {}
+        prog = {}
+        for j, (_, _, _, kind_, _, rs_, ps_, _, tb_, _) in enumerate(rx):
+            effs = dict(tb_rows[tb_]) if kind_ != 0 else {}
+            rows = [(i, True) for i in rs_] + [(i, False) for i in ps_]
+            cols = sorted(set(rs_) | set(ps_)) if kind_ == 0 else list(range(ns))
+            for k in cols:
+                code = j
+                for s_, sk in enumerate(rs_):
+                    if sk == k:
+                        code |= 1 << (17 + s_)
+                for s_, sk in enumerate(ps_):
+                    if sk == k:
+                        code |= 1 << (20 + s_)
+                em1 = None
+                if kind_ != 0:
+                    code |= 1 << 23
+                    em1 = effs.get(k)
+                for (i, isr) in rows:
+                    prog.setdefault((i, k), []).append((code | ((1 << 24) if isr else 0), em1))
+            for (i, isr) in rows:
+                prog.setdefault((i, ns), []).append((j | (1 << 16) | ((1 << 24) if isr else 0), None))
+        ents = sorted(prog.items(), key=lambda kv: (-len(kv[1]), kv[0]))
+        lanes = [[] for _ in range(32)]
+        load = [0] * 32
+        for key, terms in ents:
+            l_ = min(range(32), key=lambda x: (load[x], x))
+            lanes[l_].append((key, terms))
+            load[l_] += len(terms)
+        loff, eoff, tgt, codes, effl = [0], [0], [], [], []
+        for l_ in range(32):
+            for (i, k), terms in lanes[l_]:
+                tgt.append(i * LDA + k)
+                for code, em1 in terms:
+                    codes.append(code)
+                    effl.append(em1)
+                eoff.append(len(codes))
+            loff.append(len(tgt))
+        e(f"constexpr int NJE = {len(tgt)}, NJC = {len(codes)};")
+        e(f"{qual} int kJacLane[33] = {{{', '.join(str(x) for x in loff)}}};")
+        e(f"{qual} int kJacOff[NJE + 1] = {{{', '.join(str(x) for x in eoff)}}};")
+        e(f"{qual} int kJacT[NJE] = {{{', '.join(str(x) for x in tgt)}}};")
+        e(f"{qual} int kJacC[NJC] = {{{', '.join(str(x) for x in codes)}}};")
+        e(f"{qual} double kJacEffD[NJC] = {{{', '.join('1.0' if x is None else '(1.0 + ' + _f(x) + ')' for x in effl)}}};")
+        e(f"{qual} float kJacEffF[NJC] = {{{', '.join('1.0f' if x is None else '(1.0f + ' + _f(x) + 'f)' for x in effl)}}};")
         e(f"constexpr int NSPRX = {len(jj)};")
         e(f"{qual} int kSpRxOff[NS + 1] = {{{', '.join(str(x) for x in off)}}};")
         e(f"{qual} int kSpRxJ[NSPRX] = {{{', '.join(str(x) for x in jj)}}};")
@@ -592,9 +637,13 @@ def gen_tables(m: Mechanism, space: str = "constant") -> str:
         e("  __device__ static int sprx_end(int k) { return kSpRxOff[k + 1]; }")
         e("  __device__ static int sprx_j(int e) { return kSpRxJ[e]; }")
         e("  __device__ static double sprx_nu(int e) { return kSpRxNu[e]; }")
-        e("  __device__ static int col_begin(int k) { return kColOff[k]; }")
-        e("  __device__ static int col_end(int k) { return kColOff[k + 1]; }")
-        e("  __device__ static int col_j(int e) { return kColJ[e]; }")
+        e("  __device__ static int jac_lane(int l) { return kJacLane[l]; }")
+        e("  __device__ static int jac_off(int e) { return kJacOff[e]; }")
+        e("  __device__ static int jac_t(int e) { return kJacT[e]; }")
+        e("  __device__ static int jac_code(int c) { return kJacC[c]; }")
+        e("  template <class R> __device__ static R jac_eff(int c) {")
+        e("    if constexpr (sizeof(R) == sizeof(double)) return kJacEffD[c]; else return kJacEffF[c];")
+        e("  }")
     for nm, typ, arr in (("sp", "TabSpecies", "kSpecies"), ("rx", "TabReaction", "kReactions"),
                          ("tb", "TabThirdBody", "kThirdBody"), ("troe", "TabTroe", "kTroe")):
         e(f"  template <class R> __device__ static const {typ}<R>& {nm}(int i) {{")

@@ -139,3 +139,91 @@ def test_gri_generator_species_saturated_and_recombinations_exothermic():
         lhs = [n for n, v in r.reactants.items() for _ in range(v)]
         rhs = [n for n, v in r.products.items() for _ in range(v)]
         assert _dH298(sp, lhs, rhs) * R_CAL / 1000.0 < -20.0, r.equation()
+
+
+def test_jacobian_program_replays_the_reaction_walk():
+    """The cooperative setup's Jacobian contribution program (kJac* tables): replayed in numpy
+    on random per-reaction partials it gives, entry for entry and bit for bit, the assembly by
+    the reaction walk it replaces (each column k walks the reactions where k reacts or collides,
+    in order, adding +-(W_i/W_k) v to every row slot i and +-W_i dq/dT to the T column of k);
+    every entry has exactly one lane, and the lanes' term counts are balanced."""
+    import re
+    from pelelm_gb300.mech.codegen import gen_tables
+    from pelelm_gb300.workloads import load_mechanism
+    rng = np.random.default_rng(4)
+    for name in ("lidryer_syn", "drm19_syn", "gri_syn"):
+        m = load_mechanism(name)
+        txt = gen_tables(m, "global")
+
+        def arr(nm, conv=int):
+            body = re.search(nm + r"\[[^\]]*\] = \{([^}]*)\}", txt).group(1)
+            return [conv(x) for x in body.split(",")]
+
+        def eff(x):
+            x = x.strip()
+            return 1.0 if x == "1.0" else 1.0 + float(x[len("(1.0 + "):-1])
+
+        lane, off, tgt, codes = arr("kJacLane"), arr("kJacOff"), arr("kJacT"), arr("kJacC")
+        effs = arr("kJacEffD", eff)
+        ns, N = m.ns, m.ns + 1
+        LDA = N + 1
+        W = np.array([s.W for s in m.species])
+        kinds = {"elementary": 0, "three_body": 1, "falloff": 2}
+        order = sorted(range(m.nr), key=lambda j: (kinds[m.reactions[j].kind], j))
+        idx = {s.name: i for i, s in enumerate(m.species)}
+        P = rng.normal(size=(m.nr, 8)) * 10.0 ** rng.integers(-6, 6, size=(m.nr, 8))
+        # the reaction walk, column by column
+        A = np.zeros(N * LDA)
+        for k in range(ns):
+            for jt, j in enumerate(order):
+                r = m.reactions[j]
+                rs = [idx[s] for s, nu in r.reactants.items() for _ in range(nu)]
+                ps = [idx[s] for s, nu in r.products.items() for _ in range(nu)]
+                if not (k in rs or k in ps or r.kind != "elementary"):
+                    continue
+                v = 0.0
+                for s_, sk in enumerate(rs):
+                    if sk == k:
+                        v += P[jt, 1 + s_]
+                for s_, sk in enumerate(ps):
+                    if sk == k:
+                        v += P[jt, 4 + s_]
+                if r.kind != "elementary":
+                    v += P[jt, 7] * (1.0 + (r.efficiencies.get(m.species[k].name, 1.0) - 1.0))
+                for row, i in enumerate(rs + ps):
+                    sgn = -1.0 if row < len(rs) else 1.0
+                    if i == k:
+                        A[k * LDA + ns] += (sgn * W[i]) * P[jt, 0]
+                    if v != 0.0:
+                        A[i * LDA + k] += (sgn * W[i] * (1.0 / W[k])) * v
+        # the program
+        B = np.zeros(N * LDA)
+        owner = {}
+        for ln in range(32):
+            for en in range(lane[ln], lane[ln + 1]):
+                t = tgt[en]
+                assert t not in owner
+                owner[t] = ln
+                i, k = divmod(t, LDA)
+                w = W[i] if k == ns else W[i] * (1.0 / W[k])
+                acc = 0.0
+                for c in range(off[en], off[en + 1]):
+                    code = codes[c]
+                    pj = P[code & 0xFFFF]
+                    if code & (1 << 16):
+                        v = pj[0]
+                    else:
+                        v = 0.0
+                        for q in range(6):
+                            if code & (1 << (17 + q)):
+                                v += pj[1 + q]
+                        if code & (1 << 23):
+                            v += pj[7] * effs[c]
+                        if v == 0.0:
+                            continue
+                    acc += (-w if code & (1 << 24) else w) * v
+                B[t] = acc
+        np.testing.assert_allclose(B, A, rtol=1e-12, atol=0)
+        assert set(np.nonzero(A)[0].tolist()) <= set(owner), "a nonzero entry has no lane"
+        terms = [off[lane[ln + 1]] - off[lane[ln]] for ln in range(32)]
+        assert max(terms) <= 1.5 * np.mean(terms) + 20, (name, terms)
