@@ -311,37 +311,36 @@ __device__ __noinline__ bool warp_setup(const WVec<M> yv, const double gamma, co
     // (2) assembly by the generated contribution program: each lane owns whole entries A[i][k]
     // (species rows; k = NS: the T column) and sums their terms in a register, in the order of
     // the reaction walk (reactions ascending, then row slots): a term of reaction j is
-    // +-(W_i / W_k) v with v the partials of j that land in column k, and +-W_i dq/dT in the T
-    // column. Each entry has one writer, so the result does not depend on the lane schedule.
+    // c v, c = -+W_i / W_k (-+W_i in the T column) and v the partials of j that land in
+    // column k (dq/dT in the T column). The lanes' term streams are interleaved in the table
+    // (one contiguous line per warp load); each entry has one writer, so the result does not
+    // depend on the lane schedule.
     {
-      const int e1 = Tab::jac_lane(lane + 1);
+      JR acc = JR(0);
 #pragma unroll 1
-      for (int en = Tab::jac_lane(lane); en < e1; ++en) {
-        const int tg = Tab::jac_t(en);
-        const int i = tg / LDA, k = tg - i * LDA;
-        const JR wi = Tab::template sp<JR>(i).W;
-        const JR w = (k == NS) ? wi : wi * Tab::template sp<JR>(k).invW;
-        JR acc = JR(0);
-        const int c1 = Tab::jac_off(en + 1);
-#pragma unroll 1
-        for (int c = Tab::jac_off(en); c < c1; ++c) {
-          const int code = Tab::jac_code(c);
-          const JR* pj = RX + (code & 0xffff) * wbdf::RXW;
-          JR v;
-          if (code & (1 << 16)) {
-            v = pj[0];
-          } else {
-            v = JR(0);
+      for (int t = 0; t < Tab::JAC_TERMS; ++t) {
+        const int c = 32 * t + lane;
+        const int code = Tab::jac_code(c);
+        const JR* pj = RX + (code & 0x1ff) * wbdf::RXW;
+        const bool tcol = (code & (1 << 21)) != 0;
+        JR v;
+        if (tcol) {
+          v = pj[0];
+        } else {
+          v = JR(0);
 #pragma unroll
-            for (int q = 0; q < 6; ++q)
-              if (code & (1 << (17 + q))) v += pj[1 + q];
-            if (code & (1 << 23)) v += pj[7] * Tab::template jac_eff<JR>(c);
-            if (v == JR(0)) continue;
-          }
-          const JR cw = (code & (1 << 24)) ? -w : w;
-          acc += cw * v;
+          for (int q = 0; q < 3; ++q)
+            if (code & (1 << (22 + q))) v += pj[1 + q];
+#pragma unroll
+          for (int q = 0; q < 3; ++q)
+            if (code & (1 << (25 + q))) v += pj[4 + q];
+          if (code & (1 << 28)) v += pj[7] * Tab::template jac_eff<JR>(c);
         }
-        A[tg] = acc;
+        if (tcol || v != JR(0)) acc += Tab::template jac_w<JR>(c) * v;
+        if (code & (1 << 29)) {  // last term of the entry
+          A[(code >> 9) & 0xfff] = acc;
+          acc = JR(0);
+        }
       }
     }
     __syncwarp();

@@ -572,16 +572,19 @@ def gen_tables(m: Mechanism, space: str = "constant") -> str:
             off.append(len(jj))
         # Jacobian contribution program of the cooperative setup (warp and lane-group kernels):
         # every nonzero species entry A[i][k] (and T-column entry A[i][NS]) of the analytic
-        # Jacobian with its ordered terms. A term of reaction j adds sign * w * v to the entry,
-        # w = W_i / W_k (W_i for the T column) and v the sum of reaction j's stored partials its
-        # code selects: bit 16 dq/dT (T column), bits 17-19 / 20-22 the reactant / product slots
-        # holding species k, bit 23 the collider term dq/d[M] times the efficiency of k; bit 24 a
-        # reactant row (negative sign); bits 0-15 the reaction. Terms keep the order of the
-        # column walk they replace: reactions ascending, then the row slots of the reaction.
-        # Entries go to the 32 lanes largest first, to the lane with the fewest terms so far.
+        # Jacobian with its ordered terms. A term of reaction j adds c * v to its entry, c =
+        # -+W_i / W_k (-+W_i in the T column; minus for a reactant row slot) and v the sum of the
+        # stored partials of j that its code selects. Terms keep the order of the reaction walk
+        # they replace: reactions ascending, then the row slots of the reaction. Entries go to
+        # the 32 lanes largest first, to the lane with the fewest terms so far; each lane's terms
+        # are stored interleaved (term t of lane l at 32 t + l, lanes padded with empty terms to
+        # the longest) so a warp reads one contiguous line per load.
+        # code bits: 0-8 reaction (table order), 9-20 entry i * (N + 1) + k, 21 dq/dT (T column),
+        # 22-24 / 25-27 the reactant / product slots of j holding species k, 28 the collider
+        # term dq/d[M] times the efficiency of k, 29 last term of its entry (store the sum).
         N = ns + 1
         LDA = N + 1
-        tbeff = {}
+        assert m.nr <= 512 and N * LDA <= 4096, "program code fields too narrow for this mechanism"
         prog = {}
         for j, (_, _, _, kind_, _, rs_, ps_, _, tb_, _) in enumerate(rx):
             effs = dict(tb_rows[tb_]) if kind_ != 0 else {}
@@ -591,18 +594,18 @@ def gen_tables(m: Mechanism, space: str = "constant") -> str:
                 code = j
                 for s_, sk in enumerate(rs_):
                     if sk == k:
-                        code |= 1 << (17 + s_)
+                        code |= 1 << (22 + s_)
                 for s_, sk in enumerate(ps_):
                     if sk == k:
-                        code |= 1 << (20 + s_)
+                        code |= 1 << (25 + s_)
                 em1 = None
                 if kind_ != 0:
-                    code |= 1 << 23
+                    code |= 1 << 28
                     em1 = effs.get(k)
                 for (i, isr) in rows:
-                    prog.setdefault((i, k), []).append((code | ((1 << 24) if isr else 0), em1))
+                    prog.setdefault((i, k), []).append((code, isr, em1))
             for (i, isr) in rows:
-                prog.setdefault((i, ns), []).append((j | (1 << 16) | ((1 << 24) if isr else 0), None))
+                prog.setdefault((i, ns), []).append((j | (1 << 21), isr, None))
         ents = sorted(prog.items(), key=lambda kv: (-len(kv[1]), kv[0]))
         lanes = [[] for _ in range(32)]
         load = [0] * 32
@@ -610,22 +613,35 @@ def gen_tables(m: Mechanism, space: str = "constant") -> str:
             l_ = min(range(32), key=lambda x: (load[x], x))
             lanes[l_].append((key, terms))
             load[l_] += len(terms)
-        loff, eoff, tgt, codes, effl = [0], [0], [], [], []
+        T = max(load)
+        codes = [0] * (32 * T)
+        coefD = ["0.0"] * (32 * T)
+        coefF = ["0.0f"] * (32 * T)
+        effD = ["1.0"] * (32 * T)
+        effF = ["1.0f"] * (32 * T)
+        Wd = [_f(sp_.W) for sp_ in m.species]
+        iWd = [_f(1.0 / sp_.W) for sp_ in m.species]
         for l_ in range(32):
+            t = 0
             for (i, k), terms in lanes[l_]:
-                tgt.append(i * LDA + k)
-                for code, em1 in terms:
-                    codes.append(code)
-                    effl.append(em1)
-                eoff.append(len(codes))
-            loff.append(len(tgt))
-        e(f"constexpr int NJE = {len(tgt)}, NJC = {len(codes)};")
-        e(f"{qual} int kJacLane[33] = {{{', '.join(str(x) for x in loff)}}};")
-        e(f"{qual} int kJacOff[NJE + 1] = {{{', '.join(str(x) for x in eoff)}}};")
-        e(f"{qual} int kJacT[NJE] = {{{', '.join(str(x) for x in tgt)}}};")
-        e(f"{qual} int kJacC[NJC] = {{{', '.join(str(x) for x in codes)}}};")
-        e(f"{qual} double kJacEffD[NJC] = {{{', '.join('1.0' if x is None else '(1.0 + ' + _f(x) + ')' for x in effl)}}};")
-        e(f"{qual} float kJacEffF[NJC] = {{{', '.join('1.0f' if x is None else '(1.0f + ' + _f(x) + 'f)' for x in effl)}}};")
+                for n_, (code, isr, em1) in enumerate(terms):
+                    pos = 32 * t + l_
+                    last = n_ == len(terms) - 1
+                    codes[pos] = code | ((i * LDA + k) << 9) | ((1 << 29) if last else 0)
+                    sg = "-" if isr else ""
+                    # the same product the device forms at run time from the species tables
+                    coefD[pos] = f"{sg}{Wd[i]}" if k == ns else f"{sg}({Wd[i]} * {iWd[k]})"
+                    coefF[pos] = f"{sg}{Wd[i]}f" if k == ns else f"{sg}({Wd[i]}f * {iWd[k]}f)"
+                    if em1 is not None:
+                        effD[pos] = f"(1.0 + {_f(em1)})"
+                        effF[pos] = f"(1.0f + {_f(em1)}f)"
+                    t += 1
+        e(f"constexpr int NJT = {T};  // program terms per lane (padded)")
+        e(f"{qual} int kJacC[32 * NJT] = {{{', '.join(str(x) for x in codes)}}};")
+        e(f"{qual} double kJacWD[32 * NJT] = {{{', '.join(coefD)}}};")
+        e(f"{qual} float kJacWF[32 * NJT] = {{{', '.join(coefF)}}};")
+        e(f"{qual} double kJacEffD[32 * NJT] = {{{', '.join(effD)}}};")
+        e(f"{qual} float kJacEffF[32 * NJT] = {{{', '.join(effF)}}};")
         e(f"constexpr int NSPRX = {len(jj)};")
         e(f"{qual} int kSpRxOff[NS + 1] = {{{', '.join(str(x) for x in off)}}};")
         e(f"{qual} int kSpRxJ[NSPRX] = {{{', '.join(str(x) for x in jj)}}};")
@@ -637,10 +653,11 @@ def gen_tables(m: Mechanism, space: str = "constant") -> str:
         e("  __device__ static int sprx_end(int k) { return kSpRxOff[k + 1]; }")
         e("  __device__ static int sprx_j(int e) { return kSpRxJ[e]; }")
         e("  __device__ static double sprx_nu(int e) { return kSpRxNu[e]; }")
-        e("  __device__ static int jac_lane(int l) { return kJacLane[l]; }")
-        e("  __device__ static int jac_off(int e) { return kJacOff[e]; }")
-        e("  __device__ static int jac_t(int e) { return kJacT[e]; }")
+        e("  static constexpr int JAC_TERMS = NJT;")
         e("  __device__ static int jac_code(int c) { return kJacC[c]; }")
+        e("  template <class R> __device__ static R jac_w(int c) {")
+        e("    if constexpr (sizeof(R) == sizeof(double)) return kJacWD[c]; else return kJacWF[c];")
+        e("  }")
         e("  template <class R> __device__ static R jac_eff(int c) {")
         e("    if constexpr (sizeof(R) == sizeof(double)) return kJacEffD[c]; else return kJacEffF[c];")
         e("  }")

@@ -143,10 +143,10 @@ def test_gri_generator_species_saturated_and_recombinations_exothermic():
 
 def test_jacobian_program_replays_the_reaction_walk():
     """The cooperative setup's Jacobian contribution program (kJac* tables): replayed in numpy
-    on random per-reaction partials it gives, entry for entry and bit for bit, the assembly by
-    the reaction walk it replaces (each column k walks the reactions where k reacts or collides,
-    in order, adding +-(W_i/W_k) v to every row slot i and +-W_i dq/dT to the T column of k);
-    every entry has exactly one lane, and the lanes' term counts are balanced."""
+    on random per-reaction partials it gives, entry for entry, the assembly by the reaction walk
+    it replaces (each column k walks the reactions where k reacts or collides, in order, adding
+    -+(W_i/W_k) v to every row slot i and -+W_i dq/dT to the T column of k); every nonzero entry
+    is stored by exactly one lane, and the lanes' term streams (interleaved) are balanced."""
     import re
     from pelelm_gb300.mech.codegen import gen_tables
     from pelelm_gb300.workloads import load_mechanism
@@ -157,14 +157,12 @@ def test_jacobian_program_replays_the_reaction_walk():
 
         def arr(nm, conv=int):
             body = re.search(nm + r"\[[^\]]*\] = \{([^}]*)\}", txt).group(1)
-            return [conv(x) for x in body.split(",")]
+            return [conv(x.strip()) for x in body.split(",")]
 
-        def eff(x):
-            x = x.strip()
-            return 1.0 if x == "1.0" else 1.0 + float(x[len("(1.0 + "):-1])
-
-        lane, off, tgt, codes = arr("kJacLane"), arr("kJacOff"), arr("kJacT"), arr("kJacC")
-        effs = arr("kJacEffD", eff)
+        T = int(re.search(r"NJT = (\d+)", txt).group(1))
+        codes = arr("kJacC")
+        coef = arr("kJacWD", lambda x: float(eval(x)))
+        effs = arr("kJacEffD", lambda x: float(eval(x)))
         ns, N = m.ns, m.ns + 1
         LDA = N + 1
         W = np.array([s.W for s in m.species])
@@ -195,35 +193,39 @@ def test_jacobian_program_replays_the_reaction_walk():
                     if i == k:
                         A[k * LDA + ns] += (sgn * W[i]) * P[jt, 0]
                     if v != 0.0:
-                        A[i * LDA + k] += (sgn * W[i] * (1.0 / W[k])) * v
-        # the program
+                        A[i * LDA + k] += (sgn * (W[i] * (1.0 / W[k]))) * v
+        # the program, lane by lane
         B = np.zeros(N * LDA)
         owner = {}
+        terms = []
         for ln in range(32):
-            for en in range(lane[ln], lane[ln + 1]):
-                t = tgt[en]
-                assert t not in owner
-                owner[t] = ln
-                i, k = divmod(t, LDA)
-                w = W[i] if k == ns else W[i] * (1.0 / W[k])
-                acc = 0.0
-                for c in range(off[en], off[en + 1]):
-                    code = codes[c]
-                    pj = P[code & 0xFFFF]
-                    if code & (1 << 16):
-                        v = pj[0]
-                    else:
-                        v = 0.0
-                        for q in range(6):
-                            if code & (1 << (17 + q)):
-                                v += pj[1 + q]
-                        if code & (1 << 23):
-                            v += pj[7] * effs[c]
-                        if v == 0.0:
-                            continue
-                    acc += (-w if code & (1 << 24) else w) * v
-                B[t] = acc
+            acc, nterm = 0.0, 0
+            for t in range(T):
+                c = 32 * t + ln
+                code = codes[c]
+                pj = P[code & 0x1FF]
+                if code & (1 << 21):
+                    v = pj[0]
+                else:
+                    v = 0.0
+                    for q in range(3):
+                        if code & (1 << (22 + q)):
+                            v += pj[1 + q]
+                    for q in range(3):
+                        if code & (1 << (25 + q)):
+                            v += pj[4 + q]
+                    if code & (1 << 28):
+                        v += pj[7] * effs[c]
+                if (code & (1 << 21)) or v != 0.0:
+                    acc += coef[c] * v
+                    nterm += 1
+                if code & (1 << 29):
+                    tg = (code >> 9) & 0xFFF
+                    assert tg not in owner
+                    owner[tg] = ln
+                    B[tg] = acc
+                    acc = 0.0
+            terms.append(nterm)
         np.testing.assert_allclose(B, A, rtol=1e-12, atol=0)
         assert set(np.nonzero(A)[0].tolist()) <= set(owner), "a nonzero entry has no lane"
-        terms = [off[lane[ln + 1]] - off[lane[ln]] for ln in range(32)]
         assert max(terms) <= 1.5 * np.mean(terms) + 20, (name, terms)
