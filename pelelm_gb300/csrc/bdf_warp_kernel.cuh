@@ -310,19 +310,26 @@ __device__ __noinline__ bool warp_setup(const WVec<M> yv, const double gamma, co
     __syncwarp();
     // (2) assembly by the generated contribution program: each lane owns whole entries A[i][k]
     // (species rows; k = NS: the T column) and sums their terms in a register, in the order of
-    // the reaction walk (reactions ascending, then row slots): a term of reaction j is
-    // c v, c = -+W_i / W_k (-+W_i in the T column) and v the partials of j that land in
-    // column k (dq/dT in the T column). The lanes' term streams are interleaved in the table
-    // (one contiguous line per warp load); each entry has one writer, so the result does not
-    // depend on the lane schedule.
+    // the reaction walk (reactions ascending, then row slots): a term of reaction j is c v,
+    // c = -+W_i / W_k (-+W_i in the T column) and v the partials of j that land in column k
+    // (dq/dT in the T column). The lanes' 4-byte term codes are interleaved in the table (one
+    // contiguous line per warp load); each entry has one writer, so the result does not depend
+    // on the lane schedule.
     {
-      JR acc = JR(0);
+      JR acc = JR(0), w = JR(0);
 #pragma unroll 1
       for (int t = 0; t < Tab::JAC_TERMS; ++t) {
         const int c = 32 * t + lane;
-        const int code = Tab::jac_code(c);
+        const unsigned code = Tab::jac_code(c);
+        const bool neg = (Tab::jac_neg(t) >> lane) & 1u;
+        if (code & (1u << 30)) {  // first term of an entry: its coefficient magnitude
+          const int tg = (code >> 9) & 0xfff;
+          const int i = tg / LDA, k = tg - i * LDA;
+          const JR wi = Tab::template sp<JR>(i).W;
+          w = (k == NS) ? wi : wi * Tab::template sp<JR>(k).invW;
+        }
         const JR* pj = RX + (code & 0x1ff) * wbdf::RXW;
-        const bool tcol = (code & (1 << 21)) != 0;
+        const bool tcol = (code & (1u << 21)) != 0;
         JR v;
         if (tcol) {
           v = pj[0];
@@ -330,14 +337,14 @@ __device__ __noinline__ bool warp_setup(const WVec<M> yv, const double gamma, co
           v = JR(0);
 #pragma unroll
           for (int q = 0; q < 3; ++q)
-            if (code & (1 << (22 + q))) v += pj[1 + q];
+            if (code & (1u << (22 + q))) v += pj[1 + q];
 #pragma unroll
           for (int q = 0; q < 3; ++q)
-            if (code & (1 << (25 + q))) v += pj[4 + q];
-          if (code & (1 << 28)) v += pj[7] * Tab::template jac_eff<JR>(c);
+            if (code & (1u << (25 + q))) v += pj[4 + q];
+          if (code & (1u << 28)) v += pj[7] * ((code & (1u << 31)) ? Tab::template jac_eff<JR>(c) : JR(1));
         }
-        if (tcol || v != JR(0)) acc += Tab::template jac_w<JR>(c) * v;
-        if (code & (1 << 29)) {  // last term of the entry
+        if (tcol || v != JR(0)) acc += (neg ? -w : w) * v;
+        if (code & (1u << 29)) {  // last term of the entry
           A[(code >> 9) & 0xfff] = acc;
           acc = JR(0);
         }

@@ -578,10 +578,14 @@ def gen_tables(m: Mechanism, space: str = "constant") -> str:
         # they replace: reactions ascending, then the row slots of the reaction. Entries go to
         # the 32 lanes largest first, to the lane with the fewest terms so far; each lane's terms
         # are stored interleaved (term t of lane l at 32 t + l, lanes padded with empty terms to
-        # the longest) so a warp reads one contiguous line per load.
+        # the longest) so a warp reads one contiguous line per load. Only the 4-byte codes are
+        # streamed per setup: W_i / W_k comes from the species table at an entry's first term,
+        # and a collider efficiency is read only where it differs from 1.
         # code bits: 0-8 reaction (table order), 9-20 entry i * (N + 1) + k, 21 dq/dT (T column),
         # 22-24 / 25-27 the reactant / product slots of j holding species k, 28 the collider
-        # term dq/d[M] times the efficiency of k, 29 last term of its entry (store the sum).
+        # term dq/d[M] times the efficiency of k, 29 last term of its entry (store the sum), 30
+        # first term of its entry, 31 efficiency different from 1 (read it); the sign of c is
+        # carried by bit 29 of a separate bit plane (kJacNeg, one bit per term).
         N = ns + 1
         LDA = N + 1
         assert m.nr <= 512 and N * LDA <= 4096, "program code fields too narrow for this mechanism"
@@ -602,6 +606,8 @@ def gen_tables(m: Mechanism, space: str = "constant") -> str:
                 if kind_ != 0:
                     code |= 1 << 28
                     em1 = effs.get(k)
+                    if em1 is not None:
+                        code |= 1 << 31
                 for (i, isr) in rows:
                     prog.setdefault((i, k), []).append((code, isr, em1))
             for (i, isr) in rows:
@@ -615,31 +621,25 @@ def gen_tables(m: Mechanism, space: str = "constant") -> str:
             load[l_] += len(terms)
         T = max(load)
         codes = [0] * (32 * T)
-        coefD = ["0.0"] * (32 * T)
-        coefF = ["0.0f"] * (32 * T)
+        neg = [0] * T  # bit l of word t: term t of lane l has a reactant row slot (c < 0)
         effD = ["1.0"] * (32 * T)
         effF = ["1.0f"] * (32 * T)
-        Wd = [_f(sp_.W) for sp_ in m.species]
-        iWd = [_f(1.0 / sp_.W) for sp_ in m.species]
         for l_ in range(32):
             t = 0
             for (i, k), terms in lanes[l_]:
                 for n_, (code, isr, em1) in enumerate(terms):
                     pos = 32 * t + l_
-                    last = n_ == len(terms) - 1
-                    codes[pos] = code | ((i * LDA + k) << 9) | ((1 << 29) if last else 0)
-                    sg = "-" if isr else ""
-                    # the same product the device forms at run time from the species tables
-                    coefD[pos] = f"{sg}{Wd[i]}" if k == ns else f"{sg}({Wd[i]} * {iWd[k]})"
-                    coefF[pos] = f"{sg}{Wd[i]}f" if k == ns else f"{sg}({Wd[i]}f * {iWd[k]}f)"
+                    flags = ((1 << 29) if n_ == len(terms) - 1 else 0) | ((1 << 30) if n_ == 0 else 0)
+                    codes[pos] = (code | ((i * LDA + k) << 9) | flags) & 0xFFFFFFFF
+                    if isr:
+                        neg[t] |= 1 << l_
                     if em1 is not None:
                         effD[pos] = f"(1.0 + {_f(em1)})"
                         effF[pos] = f"(1.0f + {_f(em1)}f)"
                     t += 1
         e(f"constexpr int NJT = {T};  // program terms per lane (padded)")
-        e(f"{qual} int kJacC[32 * NJT] = {{{', '.join(str(x) for x in codes)}}};")
-        e(f"{qual} double kJacWD[32 * NJT] = {{{', '.join(coefD)}}};")
-        e(f"{qual} float kJacWF[32 * NJT] = {{{', '.join(coefF)}}};")
+        e(f"{qual} unsigned kJacC[32 * NJT] = {{{', '.join(str(x) + 'u' for x in codes)}}};")
+        e(f"{qual} unsigned kJacNeg[NJT] = {{{', '.join(str(x) + 'u' for x in neg)}}};")
         e(f"{qual} double kJacEffD[32 * NJT] = {{{', '.join(effD)}}};")
         e(f"{qual} float kJacEffF[32 * NJT] = {{{', '.join(effF)}}};")
         e(f"constexpr int NSPRX = {len(jj)};")
@@ -654,10 +654,8 @@ def gen_tables(m: Mechanism, space: str = "constant") -> str:
         e("  __device__ static int sprx_j(int e) { return kSpRxJ[e]; }")
         e("  __device__ static double sprx_nu(int e) { return kSpRxNu[e]; }")
         e("  static constexpr int JAC_TERMS = NJT;")
-        e("  __device__ static int jac_code(int c) { return kJacC[c]; }")
-        e("  template <class R> __device__ static R jac_w(int c) {")
-        e("    if constexpr (sizeof(R) == sizeof(double)) return kJacWD[c]; else return kJacWF[c];")
-        e("  }")
+        e("  __device__ static unsigned jac_code(int c) { return kJacC[c]; }")
+        e("  __device__ static unsigned jac_neg(int t) { return kJacNeg[t]; }")
         e("  template <class R> __device__ static R jac_eff(int c) {")
         e("    if constexpr (sizeof(R) == sizeof(double)) return kJacEffD[c]; else return kJacEffF[c];")
         e("  }")

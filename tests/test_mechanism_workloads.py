@@ -160,8 +160,8 @@ def test_jacobian_program_replays_the_reaction_walk():
             return [conv(x.strip()) for x in body.split(",")]
 
         T = int(re.search(r"NJT = (\d+)", txt).group(1))
-        codes = arr("kJacC")
-        coef = arr("kJacWD", lambda x: float(eval(x)))
+        codes = arr("kJacC", lambda x: int(x.rstrip("u")))
+        negs = arr("kJacNeg", lambda x: int(x.rstrip("u")))
         effs = arr("kJacEffD", lambda x: float(eval(x)))
         ns, N = m.ns, m.ns + 1
         LDA = N + 1
@@ -199,10 +199,13 @@ def test_jacobian_program_replays_the_reaction_walk():
         owner = {}
         terms = []
         for ln in range(32):
-            acc, nterm = 0.0, 0
+            acc, nterm, w = 0.0, 0, 0.0
             for t in range(T):
                 c = 32 * t + ln
                 code = codes[c]
+                if code & (1 << 30):
+                    i, k = divmod((code >> 9) & 0xFFF, LDA)
+                    w = W[i] if k == ns else W[i] * (1.0 / W[k])
                 pj = P[code & 0x1FF]
                 if code & (1 << 21):
                     v = pj[0]
@@ -215,9 +218,9 @@ def test_jacobian_program_replays_the_reaction_walk():
                         if code & (1 << (25 + q)):
                             v += pj[4 + q]
                     if code & (1 << 28):
-                        v += pj[7] * effs[c]
+                        v += pj[7] * (effs[c] if code & (1 << 31) else 1.0)
                 if (code & (1 << 21)) or v != 0.0:
-                    acc += coef[c] * v
+                    acc += (-w if (negs[t] >> ln) & 1 else w) * v
                     nterm += 1
                 if code & (1 << 29):
                     tg = (code >> 9) & 0xFFF
