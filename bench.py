@@ -621,7 +621,7 @@ WORKLOAD_TEXT = {
 
 # DRAM bytes per cell of one BDF launch (dram__bytes_read.sum + dram__bytes_write.sum of an ncu
 # capture of a smaller launch of the same kernel, divided by its cells; profiles/)
-TRAFFIC_PER_CELL = {"lidryer_syn": 22.81e6 / 131072, "drm19_syn": (12.141568e6 + 0.060928e6) / 32768}
+TRAFFIC_PER_CELL = {"lidryer_syn": 22.81e6 / 131072, "drm19_syn": (12.076800e6 + 0.017408e6) / 32768}
 
 
 def measured_peaks():
