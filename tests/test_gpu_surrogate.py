@@ -330,4 +330,10 @@ def test_surrogate_gain_over_plain_bdf(native_lib, cuda):
                          "accept": float(acc.mean()), "work_saved": sv, "plain_s": tp, "surrogate_s": ts,
                          "speedup": tp / ts, "sst": sst})
         assert ts <= 1.05 * tp * (1.0 - sv) + 0.02
+        if lv["tol_T"] == TOL_T and lv["tol_Y"] == TOL_Y:
+            # the benchmark's 1 K / 1e-4 point: calibrated on a million held-out cells, the gates
+            # keep no cell whose error could exceed the bar, so the gain there is the plain
+            # BDF's speed less the inference pass, and any accepted cell is within the bar
+            _check_fallback_and_accepted(gp, gs, sst, TOL_T, TOL_Y, "gain_at_1K")
+            assert tp / ts >= 0.95, f"surrogate + fallback at 1 K runs at {tp / ts:.3f} of the plain BDF"
     assert saved[-1] > 0.0
