@@ -22,9 +22,10 @@
 //    whole warp (warp_setup of bdf_warp_kernel.cuh, the same arithmetic as the warp mapping)
 //    into the cell's matrix in shared memory; the triangular solves run per group (rows over
 //    the group's lanes), the same operations in the same order as the warp mapping's solve;
-//  * per cell in shared memory: Nordsieck history (+ saved correction), forcing, the RHS
-//    scratch (concentrations, g/RT, rates of progress), l and tau, the matrix and its pivots;
-//    per warp: the Jacobian scratch (per-reaction partials, NASA-7 terms);
+//  * per cell in shared memory: Nordsieck history (+ saved correction), forcing, l and tau,
+//    the matrix and its pivots; per warp one region that holds the cells' RHS scratch
+//    (concentrations, g/RT, rates of progress) during the RHS and the Jacobian scratch
+//    (per-reaction partials, NASA-7 terms) during the setups;
 //  * a group whose cell is done takes the next cell index from the global queue (one atomic
 //    per warp for all groups that need a cell: work stealing across all boxes);
 //  * with a retry list (mixed precision), a failed cell is listed and left untouched for the
@@ -36,22 +37,35 @@
 
 namespace pgb {
 
-// Bytes of shared memory per cell (group) and per warp (Jacobian scratch).
+// Bytes of shared memory per cell (state that lives across passes), per cell of RHS scratch
+// (concentrations, g/RT, rates of progress: live only inside group_rhs) and per warp. The RHS
+// scratch of the warp's cells and the Jacobian scratch of the cooperative setup share one region:
+// every pass evaluates the right-hand sides first and runs the setups after them, never both at
+// once, and 3.3 KB less per warp (drm19) leaves room for more cells or more L1 for the tables.
 template <class M, class JR>
 __host__ __device__ constexpr int gbdf_cell_bytes() {
-  constexpr int N = M::N, NS = M::NS, NR = M::NR;
-  constexpr int nd = (QMAX + 2) * N + N + 2 * NS + NR + (QMAX + 1) + (QMAX + 2);
+  constexpr int N = M::N;
+  constexpr int nd = (QMAX + 2) * N + N + (QMAX + 1) + (QMAX + 2);
   constexpr int nj = N * (N + 1) + N;
   return (nd * 8 + nj * (int)sizeof(JR) + N * 4 + 15) / 16 * 16;
 }
+template <class M>
+__host__ __device__ constexpr int gbdf_rhs_bytes() {
+  return (2 * M::NS + M::NR) * 8;
+}
 template <class M, class JR>
-__host__ __device__ constexpr int gbdf_warp_scratch_bytes() {
+__host__ __device__ constexpr int gbdf_setup_bytes() {
   constexpr int N = M::N, NS = M::NS, NR = M::NR;
-  return (N * 8 + (N + wbdf::RXW * NR + 4 * NS) * (int)sizeof(JR) + 15) / 16 * 16;
+  return N * 8 + (N + wbdf::RXW * NR + 4 * NS) * (int)sizeof(JR);
+}
+template <class M, class JR, int G>
+__host__ __device__ constexpr int gbdf_shared_scratch_bytes() {
+  constexpr int a = (32 / G) * gbdf_rhs_bytes<M>(), b = gbdf_setup_bytes<M, JR>();
+  return ((a > b ? a : b) + 15) / 16 * 16;
 }
 template <class M, class JR, int G>
 __host__ __device__ constexpr int gbdf_smem_per_warp() {
-  return (32 / G) * gbdf_cell_bytes<M, JR>() + gbdf_warp_scratch_bytes<M, JR>();
+  return (32 / G) * gbdf_cell_bytes<M, JR>() + gbdf_shared_scratch_bytes<M, JR, G>();
 }
 
 // The group-distributed part of a length-N vector (element i in sub-lane i % G, slot i / G).
@@ -118,46 +132,7 @@ __device__ __noinline__ GVec<M, G> group_rhs(const GVec<M, G> yv, double* CS, do
   const double Ctot = group_sum<G>(c_loc, gm);
   __syncwarp(gm);
   for (int j = sub; j < NR; j += G) {
-    const TabReaction<double>& rx = Tab::template rx<double>(j);
-    const double lnkf = fma(rx.beta, lnT, fma(rx.mEaR, invT, rx.lnA));
-    double kf = pgb_exp64(lnkf);
-    double Mc = 1.0;
-    if (rx.tb >= 0) {
-      const TabThirdBody<double>& tb = Tab::template tb<double>(rx.tb);
-      Mc = Ctot;
-      for (int e = 0; e < tb.n; ++e) Mc = fma(tb.effm1[e], CS[tb.sp[e]], Mc);
-    }
-    if (rx.kind == 2) {
-      const TabTroe<double>& fo = Tab::template troe<double>(rx.troe);
-      const double lnk0 = fma(fo.beta0, lnT, fma(fo.mEa0R, invT, fo.lnA0));
-      const double Pr = Mc * pgb_exp64(lnk0 - lnkf);
-      double blend = Pr / (1.0 + Pr);
-      if (fo.ntroe > 0) {
-        double Fcent = fma(fo.one_m_a, pgb_exp64(T * fo.m_invT3), fo.a * pgb_exp64(T * fo.m_invT1));
-        if (fo.ntroe > 3) Fcent += pgb_exp64(invT * fo.m_T2);
-        const double lFc = pgb_log64(Fcent) * 0.4342944819032518;
-        const double cc = fma(-0.67, lFc, -0.4), nn = fma(-1.27, lFc, 0.75);
-        const double lPr = pgb_log64(fmax(Pr, 1e-300)) * 0.4342944819032518 + cc;
-        const double f1 = lPr / fma(-0.14, lPr, nn);
-        blend *= pgb_exp64(2.302585092994046 * lFc / fma(f1, f1, 1.0));
-      }
-      kf *= blend;
-    }
-    double Pf = 1.0, Pp = 1.0;
-    for (int s = 0; s < rx.nr; ++s) Pf *= CS[rx.rs[s]];
-    for (int s = 0; s < rx.np; ++s) Pp *= CS[rx.ps[s]];
-    double q;
-    if (rx.rev) {
-      double dG = -rx.dnu * lnP0RT;
-      for (int s = 0; s < rx.np; ++s) dG += GS[rx.ps[s]];
-      for (int s = 0; s < rx.nr; ++s) dG -= GS[rx.rs[s]];
-      const double kr = kf * pgb_exp64(fmin(dG, 700.0));  // finite: Pp = 0 gives 0, not NaN
-      q = fma(kf, Pf, -kr * Pp);
-    } else {
-      q = kf * Pf;
-    }
-    if (rx.kind == 1) q *= Mc;
-    QS[j] = q;
+    QS[j] = rate_of_progress<Tab>(j, T, invT, lnT, lnP0RT, Ctot, CS, GS);
   }
   __syncwarp(gm);
   double hs = 0.0, rcp = 0.0;
@@ -168,6 +143,7 @@ __device__ __noinline__ GVec<M, G> group_rhs(const GVec<M, G> yv, double* CS, do
     if (k < NS) {
       double wdot = 0.0;
       const int e1 = Tab::sprx_end(k);
+#pragma unroll 4
       for (int e = Tab::sprx_begin(k); e < e1; ++e) wdot = fma(Tab::sprx_nu(e), QS[Tab::sprx_j(e)], wdot);
       const TabSpecies<double>& s = Tab::template sp<double>(k);
       const double wm = fma(wdot, s.W, FRC[k]);
@@ -208,6 +184,7 @@ __global__ void __launch_bounds__(WPB * 32, 1) bdf_group_kernel(const ReactParam
   const unsigned gm = group_mask<G>();
   unsigned char* wbase = gsmem + (size_t)wid * gbdf_smem_per_warp<M, JR, G>();
   auto cell_base = [&](int g) { return wbase + (size_t)g * gbdf_cell_bytes<M, JR>(); };
+  unsigned char* const wscratch = cell_base(CPW);  // RHS scratch of the cells | setup scratch
   struct CellMem {
     double *Z, *FRC, *CS, *GS, *QS, *LC, *TAU;
     JR *A, *XS;
@@ -217,10 +194,10 @@ __global__ void __launch_bounds__(WPB * 32, 1) bdf_group_kernel(const ReactParam
     CellMem c;
     c.Z = reinterpret_cast<double*>(cell_base(g));  // [(QMAX+2)][N]; column QMAX+1: saved acor
     c.FRC = c.Z + (QMAX + 2) * N;                   // [N] forcing (rhoY, then rho h)
-    c.CS = c.FRC + N;                               // [NS] concentrations
+    c.CS = reinterpret_cast<double*>(wscratch + (size_t)g * gbdf_rhs_bytes<M>());  // [NS] concentrations
     c.GS = c.CS + NS;                               // [NS] g/RT
     c.QS = c.GS + NS;                               // [NR] rates of progress
-    c.LC = c.QS + NR;                               // [QMAX+1] l coefficients
+    c.LC = c.FRC + N;                               // [QMAX+1] l coefficients
     c.TAU = c.LC + (QMAX + 1);                      // [QMAX+2] step history
     c.A = reinterpret_cast<JR*>(c.TAU + (QMAX + 2));  // [N][LDA] matrix, then its LU
     c.XS = c.A + N * LDA;                           // [N] solve vector
@@ -228,7 +205,7 @@ __global__ void __launch_bounds__(WPB * 32, 1) bdf_group_kernel(const ReactParam
     return c;
   };
   const CellMem C = cell_mem(grp);
-  double* const YS = reinterpret_cast<double*>(cell_base(CPW));  // [N] setup input staging
+  double* const YS = reinterpret_cast<double*>(wscratch);         // [N] setup input staging
   JR* const WXS = reinterpret_cast<JR*>(YS + N);                  // [N] setup concentrations
   JR* const WRX = WXS + N;                                        // [NR][RXW] Jacobian partials
   JR* const WTH = WRX + wbdf::RXW * NR;                           // [4][NS] NASA-7 terms
@@ -525,7 +502,7 @@ __global__ void __launch_bounds__(WPB * 32, 1) bdf_group_kernel(const ReactParam
   };
   auto fail_cell = [&](int st) {
     status = st;
-    finish_cell();
+    phase = FINISH;
   };
   // loads flat cell c into the group; false for a covered cell (FC = 0, I_R = -F written)
   auto load_cell = [&](long long c) -> bool {
@@ -817,7 +794,7 @@ __global__ void __launch_bounds__(WPB * 32, 1) bdf_group_kernel(const ReactParam
               qwait = 10;
               phase = RESETD;
             }
-            if (phase != NEED && fabs(h) <= 100.0 * UROUND * fabs(t)) fail_cell(HSMALL);
+            if (phase != FINISH && fabs(h) <= 100.0 * UROUND * fabs(t)) fail_cell(HSMALL);
           }
         } else {
           // ---- step accepted: complete it ----
@@ -842,7 +819,7 @@ __global__ void __launch_bounds__(WPB * 32, 1) bdf_group_kernel(const ReactParam
             tq5_saved = tq5;
           }
           if (fabs(t - tout) <= 100.0 * UROUND * (fabs(t) + fabs(h)) || t >= tout) {
-            finish_cell();
+            phase = FINISH;
           } else {
             // ---- next step size and order ----
             const double etaq = 1.0 / (pgb_pow64((BIAS2 * BIAS2) * dsm2, 0.5 * inv_int(q + 1)) + ADDON);
@@ -907,6 +884,8 @@ __global__ void __launch_bounds__(WPB * 32, 1) bdf_group_kernel(const ReactParam
         }
       }
     }
+    // ------------------------------------------------ (F) write back a finished cell
+    if (phase == FINISH) finish_cell();
     __syncwarp();
   }
 }

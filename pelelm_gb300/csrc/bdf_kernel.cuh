@@ -42,7 +42,10 @@ constexpr int SMALL_NST = 10, MXNEF = 7, MXNEF1 = 3, SMALL_NEF = 2, MXNCF = 10;
 constexpr int MAXCOR = 3, MSBP = 20;
 constexpr double CRDOWN = 0.3, RDIV = 2.0, DGMAX = 0.3, NLSCOEF = 0.1;
 
-enum Phase : int { IDLE = 0, NEED = 1, START = 2, HIN = 3, STEP = 4, NEWTON = 5, RESETD = 6 };
+// FINISH: the cell's integration has ended (status set) and its write-back is pending; the
+// group kernel runs that write-back from one place at the end of a pass (the per-thread kernel,
+// whose cells finish where they end, does not use it).
+enum Phase : int { IDLE = 0, NEED = 1, FINISH = 2, START = 3, HIN = 4, STEP = 5, NEWTON = 6, RESETD = 7 };
 
 // 1/j for the small integers the order logic divides by (no FP64 division on the device)
 __device__ __forceinline__ double inv_int(int j) {

@@ -70,6 +70,61 @@ struct WVec {
   double v[(M::N + 31) / 32];
 };
 
+// Rate of progress of reaction j (table order) at one state, FP64: the equations of the table
+// RHS in mech_tables.cuh (Arrhenius forward rate, third-body and Lindemann/Troe fall-off
+// factors, reverse rate from K_c with the exponent capped at 700), the same operations in the
+// same order. Shared by the warp and lane-group right-hand sides.
+template <class Tab>
+__device__ __forceinline__ double rate_of_progress(int j, double T, double invT, double lnT, double lnP0RT,
+                                                   double Ctot, const double* CS, const double* GS) {
+  const TabReaction<double>& rx = Tab::template rx<double>(j);
+  const double lnkf = fma(rx.beta, lnT, fma(rx.mEaR, invT, rx.lnA));
+  double kf = pgb_exp64(lnkf);
+  double Mc = 1.0;
+  if (rx.tb >= 0) {
+    const TabThirdBody<double>& tb = Tab::template tb<double>(rx.tb);
+    Mc = Ctot;
+#pragma unroll
+    for (int e = 0; e < 8; ++e)
+      if (e < tb.n) Mc = fma(tb.effm1[e], CS[tb.sp[e]], Mc);
+  }
+  if (rx.kind == 2) {
+    const TabTroe<double>& fo = Tab::template troe<double>(rx.troe);
+    const double lnk0 = fma(fo.beta0, lnT, fma(fo.mEa0R, invT, fo.lnA0));
+    const double Pr = Mc * pgb_exp64(lnk0 - lnkf);
+    double blend = Pr / (1.0 + Pr);
+    if (fo.ntroe > 0) {
+      double Fcent = fma(fo.one_m_a, pgb_exp64(T * fo.m_invT3), fo.a * pgb_exp64(T * fo.m_invT1));
+      if (fo.ntroe > 3) Fcent += pgb_exp64(invT * fo.m_T2);
+      const double lFc = pgb_log64(Fcent) * 0.4342944819032518;
+      const double cc = fma(-0.67, lFc, -0.4), nn = fma(-1.27, lFc, 0.75);
+      const double lPr = pgb_log64(fmax(Pr, 1e-300)) * 0.4342944819032518 + cc;
+      const double f1 = lPr / fma(-0.14, lPr, nn);
+      blend *= pgb_exp64(2.302585092994046 * lFc / fma(f1, f1, 1.0));
+    }
+    kf *= blend;
+  }
+  double Pf = 1.0, Pp = 1.0;
+#pragma unroll
+  for (int s = 0; s < 3; ++s) if (s < rx.nr) Pf *= CS[rx.rs[s]];
+#pragma unroll
+  for (int s = 0; s < 3; ++s) if (s < rx.np) Pp *= CS[rx.ps[s]];
+  double q;
+  if (rx.rev) {
+    double dG = -rx.dnu * lnP0RT;
+#pragma unroll
+    for (int s = 0; s < 3; ++s) if (s < rx.np) dG += GS[rx.ps[s]];
+#pragma unroll
+    for (int s = 0; s < 3; ++s) if (s < rx.nr) dG -= GS[rx.rs[s]];
+    const double kr = kf * pgb_exp64(fmin(dG, 700.0));  // finite: Pp = 0 gives 0, not NaN
+    q = fma(kf, Pf, -kr * Pp);
+  } else {
+    q = kf * Pf;
+  }
+  if (rx.kind == 1) q *= Mc;
+  return q;
+}
+
 // Right-hand side f = [W_k wdot_k + F_k, dT/dt] at y, one warp cooperating (see the kernel
 // below). One non-inlined copy serves every call site: the step loop calls it from five places
 // and inlined copies of this exp/log-heavy body overflow the instruction cache.
@@ -108,46 +163,7 @@ __device__ __noinline__ WVec<M> warp_rhs(const WVec<M> yv, double* CS, double* G
   const double Ctot = warp_sum(c_loc);
   __syncwarp();
   for (int j = lane; j < NR; j += 32) {
-    const TabReaction<double>& rx = Tab::template rx<double>(j);
-    const double lnkf = fma(rx.beta, lnT, fma(rx.mEaR, invT, rx.lnA));
-    double kf = pgb_exp64(lnkf);
-    double Mc = 1.0;
-    if (rx.tb >= 0) {
-      const TabThirdBody<double>& tb = Tab::template tb<double>(rx.tb);
-      Mc = Ctot;
-      for (int e = 0; e < tb.n; ++e) Mc = fma(tb.effm1[e], CS[tb.sp[e]], Mc);
-    }
-    if (rx.kind == 2) {
-      const TabTroe<double>& fo = Tab::template troe<double>(rx.troe);
-      const double lnk0 = fma(fo.beta0, lnT, fma(fo.mEa0R, invT, fo.lnA0));
-      const double Pr = Mc * pgb_exp64(lnk0 - lnkf);
-      double blend = Pr / (1.0 + Pr);
-      if (fo.ntroe > 0) {
-        double Fcent = fma(fo.one_m_a, pgb_exp64(T * fo.m_invT3), fo.a * pgb_exp64(T * fo.m_invT1));
-        if (fo.ntroe > 3) Fcent += pgb_exp64(invT * fo.m_T2);
-        const double lFc = pgb_log64(Fcent) * 0.4342944819032518;
-        const double cc = fma(-0.67, lFc, -0.4), nn = fma(-1.27, lFc, 0.75);
-        const double lPr = pgb_log64(fmax(Pr, 1e-300)) * 0.4342944819032518 + cc;
-        const double f1 = lPr / fma(-0.14, lPr, nn);
-        blend *= pgb_exp64(2.302585092994046 * lFc / fma(f1, f1, 1.0));
-      }
-      kf *= blend;
-    }
-    double Pf = 1.0, Pp = 1.0;
-    for (int s = 0; s < rx.nr; ++s) Pf *= CS[rx.rs[s]];
-    for (int s = 0; s < rx.np; ++s) Pp *= CS[rx.ps[s]];
-    double q;
-    if (rx.rev) {
-      double dG = -rx.dnu * lnP0RT;
-      for (int s = 0; s < rx.np; ++s) dG += GS[rx.ps[s]];
-      for (int s = 0; s < rx.nr; ++s) dG -= GS[rx.rs[s]];
-      const double kr = kf * pgb_exp64(fmin(dG, 700.0));  // finite: Pp = 0 gives 0, not NaN
-      q = fma(kf, Pf, -kr * Pp);
-    } else {
-      q = kf * Pf;
-    }
-    if (rx.kind == 1) q *= Mc;
-    QS[j] = q;
+    QS[j] = rate_of_progress<Tab>(j, T, invT, lnT, lnP0RT, Ctot, CS, GS);
   }
   __syncwarp();
   double hs = 0.0, rcp = 0.0;
@@ -158,6 +174,7 @@ __device__ __noinline__ WVec<M> warp_rhs(const WVec<M> yv, double* CS, double* G
     if (k < NS) {
       double wdot = 0.0;
       const int e1 = Tab::sprx_end(k);
+#pragma unroll 4
       for (int e = Tab::sprx_begin(k); e < e1; ++e) wdot = fma(Tab::sprx_nu(e), QS[Tab::sprx_j(e)], wdot);
       const TabSpecies<double>& s = Tab::template sp<double>(k);
       const double wm = fma(wdot, s.W, FRC[k]);
@@ -240,7 +257,9 @@ __device__ __noinline__ bool warp_setup(const WVec<M> yv, const double gamma, co
       if (r.tb >= 0) {
         const TabThirdBody<JR>& t = Tab::template tb<JR>(r.tb);
         Mc = Ctot;
-        for (int e = 0; e < t.n; ++e) Mc += t.effm1[e] * XS[t.sp[e]];
+#pragma unroll
+        for (int e = 0; e < 8; ++e)
+          if (e < t.n) Mc += t.effm1[e] * XS[t.sp[e]];
         if (r.kind == 1) alpha = Mc;
       }
       if (r.kind == 2) {
@@ -275,14 +294,18 @@ __device__ __noinline__ bool warp_setup(const WVec<M> yv, const double gamma, co
       JR kr = JR(0), dlnkr = JR(0);
       if (r.rev) {
         JR dG = -(JR)r.dnu * lnP0RT, dH = JR(0);
-        for (int s = 0; s < r.np; ++s) {
-          dG += TG[r.ps[s]];
-          dH += TH_[r.ps[s]];
-        }
-        for (int s = 0; s < r.nr; ++s) {
-          dG -= TG[r.rs[s]];
-          dH -= TH_[r.rs[s]];
-        }
+#pragma unroll
+        for (int s = 0; s < 3; ++s)
+          if (s < r.np) {
+            dG += TG[r.ps[s]];
+            dH += TH_[r.ps[s]];
+          }
+#pragma unroll
+        for (int s = 0; s < 3; ++s)
+          if (s < r.nr) {
+            dG -= TG[r.rs[s]];
+            dH -= TH_[r.rs[s]];
+          }
         kr = kf * pgb_expT<JR>(fmin(dG, JR(700)));
         dlnkr = dlnkf - (dH - (JR)r.dnu) * invT;
       }
@@ -298,12 +321,14 @@ __device__ __noinline__ bool warp_setup(const WVec<M> yv, const double gamma, co
       if (r.kind == 1) bm = kf * Pf - kr * Pp;
       else if (r.kind == 2) bm = dkeff_dM * (Pf - (kf > JR(0) ? kr / kf : JR(0)) * Pp);
       out[7] = bm;
-      for (int row = 0; row < r.nr + r.np; ++row) {
-        const bool isr = row < r.nr;
-        const int i = isr ? r.rs[row] : r.ps[row - r.nr];
-        Qw += (isr ? -q : q) * TH_[i] * RT;
-        cpw += (isr ? -q : q) * TC[i] * JR(kRerg);
-      }
+#pragma unroll
+      for (int row = 0; row < 6; ++row)
+        if (row < r.nr + r.np) {
+          const bool isr = row < r.nr;
+          const int i = isr ? r.rs[row] : r.ps[row - r.nr];
+          Qw += (isr ? -q : q) * TH_[i] * RT;
+          cpw += (isr ? -q : q) * TC[i] * JR(kRerg);
+        }
     }
     Qw = warp_sum(Qw);
     cpw = warp_sum(cpw);
