@@ -322,6 +322,7 @@ def run_gb(args, ws, rank, local, pg):
     ncell, cs, lay, arenas = shard.ncell, shard.cs, shard.lay, shard.arenas
     sst = r.surrogate_stats() if surrogate else None
     tuning = r.tuning()
+    family = tuned_family(tuning, cfg.mech)
     t_max = allmax(pg, t_step)
     value = allsum(pg, float(ncell * args.steps)) / t_max
     ms_per_step = 1e3 * t_max / args.steps
@@ -405,11 +406,11 @@ def run_gb(args, ws, rank, local, pg):
             extra["surrogate_pareto"] = surrogate_pareto(
                 surrogate, make_reactor, sg_opts, timed_steps, work, plain_cps, ncell, pg, rank, cfg, cs, lay,
                 args.error_sample, None if args.no_error_check else error_vs_oracle)
-        dominant = "bdf_reactor_kernel (fallback cells)"
+        dominant = f"{KERNEL_OF_FAMILY[family]} (fallback cells)"
     else:
         nfe = st["nfe"]
         achieved = flops_rhs * nfe / (t_step / args.steps) / 1e12
-        dominant = "bdf_reactor_kernel"
+        dominant = KERNEL_OF_FAMILY[family]
     if not args.no_fp64_line and args.precision != "fp64":
         # the plain GPU BDF in FP64 throughout (the reference's own precision) on the same
         # workload: the like-for-like figure beside the mixed-precision one
@@ -461,8 +462,8 @@ def run_gb(args, ws, rank, local, pg):
                          "frac": achieved / fp64_peak,
                          # DRAM bytes per launch from an ncu capture of a smaller launch of the same
                          # kernel, scaled by cells (profiles/)
-                         "traffic": (TRAFFIC_PER_CELL[cfg.mech] * (sst["fallback"] if surrogate else ncell)
-                                     if cfg.mech in TRAFFIC_PER_CELL else None),
+                         "traffic": (TRAFFIC_PER_CELL[(cfg.mech, family)] * (sst["fallback"] if surrogate else ncell)
+                                     if (cfg.mech, family) in TRAFFIC_PER_CELL else None),
                          "kernel": dominant,
                          "what": f"rate evaluation: {flops_rhs} algorithmic FP64 flops per RHS "
                                  f"({ops} ops + {trans} transcendentals x {FLOPS_PER_TRANSCENDENTAL}) "
@@ -619,9 +620,25 @@ WORKLOAD_TEXT = {
               "forcing as lidryer_amr120",
 }
 
-# DRAM bytes per cell of one BDF launch (dram__bytes_read.sum + dram__bytes_write.sum of an ncu
-# capture of a smaller launch of the same kernel, divided by its cells; profiles/)
-TRAFFIC_PER_CELL = {"lidryer_syn": 22.81e6 / 131072, "drm19_syn": (12.076800e6 + 0.017408e6) / 32768}
+# DRAM bytes per cell of one BDF launch, per mechanism and kernel family (dram__bytes_read.sum +
+# dram__bytes_write.sum of an ncu capture of a smaller launch of the same kernel, divided by its
+# cells; profiles/)
+TRAFFIC_PER_CELL = {("lidryer_syn", "thread"): 22.81e6 / 131072,
+                    ("drm19_syn", "group"): (12.618496e6 + 0.043264e6) / 32768,
+                    ("drm19_syn", "warp"): (12.076800e6 + 0.017408e6) / 32768}
+KERNEL_OF_FAMILY = {"thread": "bdf_reactor_kernel", "warp": "bdf_warp_kernel", "group": "bdf_group_kernel"}
+
+
+def tuned_family(tuning: str, mech: str) -> str:
+    """Kernel family the autotuner picked ("... -> group/8"), else the library's default for the
+    mechanism's size (per thread up to 12 species, lane groups up to 31)."""
+    if "->" in tuning:
+        fam = tuning.rsplit("->", 1)[1].strip().split("/")[0]
+        if fam in KERNEL_OF_FAMILY:
+            return fam
+    from pelelm_gb300.workloads import load_mechanism
+    ns = load_mechanism(mech).ns
+    return "thread" if ns <= 12 else "group" if ns + 1 <= 32 else "warp"
 
 
 def measured_peaks():
