@@ -200,6 +200,10 @@ int pgb_rhoh_to_temp(const char* mechanism, const pgb_box_view* view, double tmi
  * - nbox must be in [1, PGB_NOALLOC_MAX_BOXES]; larger box lists are rejected with an error.
  * - The first call on a device (with that device current) resolves the scratch array's device
  *   address; make that first call before any stream capture.
+ * - Capturable: the box table reaches the scratch array through kernel parameters (no host
+ *   buffer outlives the call), so a captured call replays with the views it was captured with.
+ *   stats must be NULL while the stream is capturing (they wait for the advance); the call
+ *   returns an error otherwise.
  * - All calls on a device share the one scratch array, which keeps the last call's contents
  *   (the queue head and counters are cleared on each call). Calls whose work overlaps on the
  *   GPU — concurrent streams or threads — race on it: serialize them.

@@ -39,13 +39,25 @@ namespace wbdf {
 constexpr int RXW = 8;  // Jacobian scratch per reaction: dq/dT, 3 reactant partials, 3 product partials, [M] partial
 }
 
-// Bytes of shared memory per warp for mechanism M and Jacobian type JR.
+// Shared memory of one warp (one cell) for mechanism M and Jacobian type JR: the FP64 state
+// (Nordsieck history, forcing, l, tau), one scratch region and the matrix. The scratch region
+// holds the RHS scratch (concentrations, g/RT, rates of progress) inside warp_rhs and the setup
+// scratch (per-reaction partials, NASA-7 terms) inside warp_setup: never both live.
+template <class M>
+__host__ __device__ constexpr int bdf_warp_state_bytes() {
+  return (((QMAX + 2) * M::N + M::N + (QMAX + 1) + (QMAX + 2)) * 8 + 15) / 16 * 16;
+}
+template <class M, class JR>
+__host__ __device__ constexpr int bdf_warp_scratch_bytes() {
+  constexpr int NS = M::NS, NR = M::NR;
+  constexpr int rhs = (2 * NS + NR) * 8, setup = (wbdf::RXW * NR + 4 * NS) * (int)sizeof(JR);
+  return ((rhs > setup ? rhs : setup) + 15) / 16 * 16;
+}
 template <class M, class JR>
 __host__ __device__ constexpr int bdf_warp_smem_per_warp() {
-  constexpr int N = M::N, NS = M::NS, NR = M::NR;
-  constexpr int nd = (QMAX + 2) * N + N + 2 * NS + NR + (QMAX + 1) + (QMAX + 2);
-  constexpr int nj = N * (N + 1) + N + wbdf::RXW * NR + 4 * NS;
-  return ((nd * 8 + nj * (int)sizeof(JR) + N * 4) + 15) / 16 * 16;
+  constexpr int N = M::N;
+  constexpr int nj = N * (N + 1) + N;
+  return (bdf_warp_state_bytes<M>() + bdf_warp_scratch_bytes<M, JR>() + nj * (int)sizeof(JR) + N * 4 + 15) / 16 * 16;
 }
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -511,16 +523,17 @@ __global__ void __launch_bounds__(WPB * 32, 1) bdf_warp_kernel(const ReactParams
   unsigned char* base = wsmem + (size_t)wid * bdf_warp_smem_per_warp<M, JR>();
   double* Z = reinterpret_cast<double*>(base);   // [(QMAX+2)][N]
   double* FRC = Z + (QMAX + 2) * N;              // [N] forcing (rhoY, then rho h)
-  double* CS = FRC + N;                          // [NS] concentrations
+  double* LC = FRC + N;                          // [QMAX+1] l coefficients
+  double* TAU = LC + (QMAX + 1);                 // [QMAX+2] step history
+  unsigned char* const scratch = base + bdf_warp_state_bytes<M>();  // RHS | setup scratch
+  double* CS = reinterpret_cast<double*>(scratch);  // [NS] concentrations
   double* GS = CS + NS;                          // [NS] g/RT
   double* QS = GS + NS;                          // [NR] rates of progress
-  double* LC = QS + NR;                          // [QMAX+1] l coefficients
-  double* TAU = LC + (QMAX + 1);                 // [QMAX+2] step history
-  JR* A = reinterpret_cast<JR*>(TAU + (QMAX + 2));  // [N][LDA] Jacobian, then its LU
-  JR* XS = A + N * LDA;                          // [N] solve vector
-  JR* RX = XS + N;                               // [NR][RXW] Jacobian partials
+  JR* RX = reinterpret_cast<JR*>(scratch);       // [NR][RXW] Jacobian partials
   JR* TH = RX + wbdf::RXW * NR;                  // [4][NS] NASA-7 terms of the setup
-  int* PIV = reinterpret_cast<int*>(TH + 4 * NS);
+  JR* A = reinterpret_cast<JR*>(scratch + bdf_warp_scratch_bytes<M, JR>());  // [N][LDA] Jacobian, then its LU
+  JR* XS = A + N * LDA;                          // [N] solve vector
+  int* PIV = reinterpret_cast<int*>(XS + N);
 
   const long long ncell = P.ncell_dev ? (long long)*P.ncell_dev : P.ncell;
   const int qmax = max(1, min(P.max_order, QMAX));

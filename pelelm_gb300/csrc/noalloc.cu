@@ -99,9 +99,16 @@ extern "C" int pgb_react_boxes_noalloc(const char* mechanism, const pgb_box_view
     if (!wpb || !m->warp_mixed)
       return set_err("noalloc: no compiled kernel of mechanism '%s' keeps its state in shared memory", m->name);
   }
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  // Under stream capture the call records only stream work (box-table kernels, memsets, the
+  // advance); stats need a wait for the advance, which a capture cannot contain.
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  PGB_CUDA(cudaStreamIsCapturing(st, &cap));
+  if (cap != cudaStreamCaptureStatusNone && stats)
+    return set_err("noalloc: stats wait for the advance, which a stream capture cannot contain; "
+                   "pass stats = NULL while capturing");
   NoAllocScratch* S = nullptr;
   if (scratch_of_current_device(&S)) return -1;
-  cudaStream_t st = static_cast<cudaStream_t>(stream);
 
   // Box table: validated and converted here, copied into the scratch array through kernel
   // parameters.

@@ -102,7 +102,7 @@ constexpr int warp_wpb_choice(int i) {
     constexpr int c[] = {16, 8, 0, 0};
     return i < 4 ? c[i] : 0;
   } else {
-    constexpr int c[] = {6, 4, 0, 0};
+    constexpr int c[] = {8, 6, 4, 0};
     return i < 4 ? c[i] : 0;
   }
 }
@@ -115,6 +115,7 @@ int launch_bdf_warp(const pgb::ReactParams& p, int wpb, cudaStream_t s, int nblo
     if (wpb == 16) return launch_bdf_warp_wpb<M, JR, 16>(p, s, nblocks);
     if (wpb == 8) return launch_bdf_warp_wpb<M, JR, 8>(p, s, nblocks);
   } else {
+    if (wpb == 8) return launch_bdf_warp_wpb<M, JR, 8>(p, s, nblocks);
     if (wpb == 6) return launch_bdf_warp_wpb<M, JR, 6>(p, s, nblocks);
     if (wpb == 4) return launch_bdf_warp_wpb<M, JR, 4>(p, s, nblocks);
   }

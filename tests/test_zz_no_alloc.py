@@ -96,3 +96,41 @@ def test_noalloc_rejects_too_many_boxes(native_lib, cuda):
                                             5, 20000, 1, None, None)
     assert rc == -1
     assert "exceed" in _lib.last_error()
+
+
+@pytest.mark.gpu
+def test_noalloc_captures_and_replays(native_lib, cuda):
+    """A call captured into a CUDA graph replays to the same outputs as a direct call on the
+    same inputs (the box table travels in kernel parameters, so nothing the graph refers to
+    dies with the call); asking for stats while the stream is capturing is refused before any
+    work is recorded, and leaves the capture usable."""
+    torch = cuda
+    cfg, cs = _inputs("drm19_2M")
+    ns = cs.rY.shape[1]
+    lib = _lib.lib()
+    _noalloc(lib, cfg, boxes_from_cells(torch, cs, SHAPES, lo_list=LOS, ghost=1, with_mask=True), "mixed")
+    direct = boxes_from_cells(torch, cs, SHAPES, lo_list=LOS, ghost=1, with_mask=True)
+    _noalloc(lib, cfg, direct, "mixed")
+    ref = gather(direct, ns)
+
+    captured = boxes_from_cells(torch, cs, SHAPES, lo_list=LOS, ghost=1, with_mask=True)
+    views = (_lib.BoxView * len(captured))(*[b.view() for b in captured])
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, capture_error_mode="thread_local"):
+        sptr = torch.cuda.current_stream().cuda_stream
+        st = _lib.Stats()
+        rc = lib.pgb_react_boxes_noalloc(cfg.mech.encode(), views, len(captured), cfg.dt, cfg.rtol,
+                                         cfg.atol, 5, 20000, 0, C.c_void_p(sptr), C.byref(st))
+        assert rc == -1 and "capture" in _lib.last_error()
+        rc = lib.pgb_react_boxes_noalloc(cfg.mech.encode(), views, len(captured), cfg.dt, cfg.rtol,
+                                         cfg.atol, 5, 20000, 0, C.c_void_p(sptr), None)
+        assert rc == 0, _lib.last_error()
+    torch.cuda.synchronize()
+    before = gather(captured, ns)
+    np.testing.assert_array_equal(before[3], 0.0)  # capture records, it does not run
+    g.replay()
+    torch.cuda.synchronize()
+    out = gather(captured, ns)
+    for a, b in zip(out, ref):
+        np.testing.assert_array_equal(a, b)
