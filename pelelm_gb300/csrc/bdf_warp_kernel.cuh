@@ -85,23 +85,31 @@ struct WVec {
 // Rate of progress of reaction j (table order) at one state, FP64: the equations of the table
 // RHS in mech_tables.cuh (Arrhenius forward rate, third-body and Lindemann/Troe fall-off
 // factors, reverse rate from K_c with the exponent capped at 700), the same operations in the
-// same order. Shared by the warp and lane-group right-hand sides.
+// same order. Shared by the warp and lane-group right-hand sides; the reaction's data comes
+// from its two packed records (TabRxArr, TabRxPk: three loads instead of one per field).
 template <class Tab>
 __device__ __forceinline__ double rate_of_progress(int j, double T, double invT, double lnT, double lnP0RT,
                                                    double Ctot, const double* CS, const double* GS) {
-  const TabReaction<double>& rx = Tab::template rx<double>(j);
-  const double lnkf = fma(rx.beta, lnT, fma(rx.mEaR, invT, rx.lnA));
+  const TabRxArr& ar = Tab::rx_arr(j);
+  const TabRxPk pk = Tab::rx_pk(j);
+  const int kind = pk.x & 3u, nr = (pk.x >> 3) & 3u, np = (pk.x >> 5) & 3u;
+  const bool rev = (pk.x >> 2) & 1u;
+  const int dnu = (int)((pk.x >> 7) & 15u) - 8, tbi = (int)((pk.x >> 11) & 2047u) - 1;
+  const int troe = (int)(pk.x >> 22) - 1;
+  auto rs = [&](int s) { return (int)((pk.y >> (10 * s)) & 1023u); };
+  auto ps = [&](int s) { return (int)((pk.z >> (10 * s)) & 1023u); };
+  const double lnkf = fma(ar.beta, lnT, fma(ar.mEaR, invT, ar.lnA));
   double kf = pgb_exp64(lnkf);
   double Mc = 1.0;
-  if (rx.tb >= 0) {
-    const TabThirdBody<double>& tb = Tab::template tb<double>(rx.tb);
+  if (tbi >= 0) {
+    const TabThirdBody<double>& tb = Tab::template tb<double>(tbi);
     Mc = Ctot;
 #pragma unroll
     for (int e = 0; e < 8; ++e)
       if (e < tb.n) Mc = fma(tb.effm1[e], CS[tb.sp[e]], Mc);
   }
-  if (rx.kind == 2) {
-    const TabTroe<double>& fo = Tab::template troe<double>(rx.troe);
+  if (kind == 2) {
+    const TabTroe<double>& fo = Tab::template troe<double>(troe);
     const double lnk0 = fma(fo.beta0, lnT, fma(fo.mEa0R, invT, fo.lnA0));
     const double Pr = Mc * pgb_exp64(lnk0 - lnkf);
     double blend = Pr / (1.0 + Pr);
@@ -118,22 +126,22 @@ __device__ __forceinline__ double rate_of_progress(int j, double T, double invT,
   }
   double Pf = 1.0, Pp = 1.0;
 #pragma unroll
-  for (int s = 0; s < 3; ++s) if (s < rx.nr) Pf *= CS[rx.rs[s]];
+  for (int s = 0; s < 3; ++s) if (s < nr) Pf *= CS[rs(s)];
 #pragma unroll
-  for (int s = 0; s < 3; ++s) if (s < rx.np) Pp *= CS[rx.ps[s]];
+  for (int s = 0; s < 3; ++s) if (s < np) Pp *= CS[ps(s)];
   double q;
-  if (rx.rev) {
-    double dG = -rx.dnu * lnP0RT;
+  if (rev) {
+    double dG = -dnu * lnP0RT;
 #pragma unroll
-    for (int s = 0; s < 3; ++s) if (s < rx.np) dG += GS[rx.ps[s]];
+    for (int s = 0; s < 3; ++s) if (s < np) dG += GS[ps(s)];
 #pragma unroll
-    for (int s = 0; s < 3; ++s) if (s < rx.nr) dG -= GS[rx.rs[s]];
+    for (int s = 0; s < 3; ++s) if (s < nr) dG -= GS[rs(s)];
     const double kr = kf * pgb_exp64(fmin(dG, 700.0));  // finite: Pp = 0 gives 0, not NaN
     q = fma(kf, Pf, -kr * Pp);
   } else {
     q = kf * Pf;
   }
-  if (rx.kind == 1) q *= Mc;
+  if (kind == 1) q *= Mc;
   return q;
 }
 

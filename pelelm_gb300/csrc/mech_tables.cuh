@@ -33,6 +33,18 @@ struct TabReaction {
   int dnu, tb, troe;      // sum(nu'') - sum(nu'), third-body row or -1, falloff row or -1
 };
 
+// The FP64 rate of progress of the warp and lane-group kernels reads a reaction through two
+// aligned records instead of the fields of TabReaction one by one (the same values): the
+// Arrhenius triple, and the integer fields packed in four words —
+//   x: kind (bits 0-1), rev (2), nr (3-4), np (5-6), dnu + 8 (7-10), tb + 1 (11-21),
+//      troe + 1 (22-31);  y: rs[0..2], z: ps[0..2], 10 bits each;  w: 0.
+struct __align__(32) TabRxArr {
+  double lnA, beta, mEaR, pad;
+};
+struct __align__(16) TabRxPk {
+  unsigned x, y, z, w;
+};
+
 template <class R>
 struct TabThirdBody {
   int n;

@@ -469,6 +469,21 @@ if __name__ == "__main__":
 
 
 # ---------------------------------------------------------------------------- tables
+def rx_packed(rx, ns: int) -> list:
+    """The four words of each reaction's TabRxPk record (mech_tables.cuh): x = kind | rev << 2 |
+    nr << 3 | np << 5 | (dnu + 8) << 7 | (tb + 1) << 11 | (troe + 1) << 22; y, z = the reactant and
+    product species slots, 10 bits each; w = 0."""
+    assert ns <= 1024, "species index fields of the packed reaction record are 10 bits"
+    out = []
+    for (_, _, _, kind, rev, rs, ps, dnu, tb, tr) in rx:
+        assert -8 <= dnu <= 7 and tb + 1 < 2048 and tr + 1 < 1024
+        x = kind | rev << 2 | len(rs) << 3 | len(ps) << 5 | (dnu + 8) << 7 | (tb + 1) << 11 | (tr + 1) << 22
+        y = sum(k << (10 * s_) for s_, k in enumerate(rs))
+        z = sum(k << (10 * s_) for s_, k in enumerate(ps))
+        out.append((x, y, z, 0))
+    return out
+
+
 def gen_tables(m: Mechanism, space: str = "constant") -> str:
     """Mechanism tables for the table-driven kernels: per-species W, NASA-7 sets, per-reaction
     Arrhenius data, stoichiometry as species slots (a species with coefficient 2 occupies two
@@ -642,6 +657,15 @@ def gen_tables(m: Mechanism, space: str = "constant") -> str:
         e(f"{qual} unsigned kJacNeg[NJT] = {{{', '.join(str(x) + 'u' for x in neg)}}};")
         e(f"{qual} double kJacEffD[32 * NJT] = {{{', '.join(effD)}}};")
         e(f"{qual} float kJacEffF[32 * NJT] = {{{', '.join(effF)}}};")
+        # packed reaction records of the FP64 rate of progress (TabRxArr / TabRxPk)
+        e(f"{qual} TabRxArr kRxArr[NR] = {{")
+        for (lnA, beta, mear, *_r) in rx:
+            e(f"  {{{_f(lnA)}, {_f(beta)}, {_f(mear)}, 0.0}},")
+        e("};")
+        e(f"{qual} TabRxPk kRxPk[NR] = {{")
+        for w in rx_packed(rx, ns):
+            e("  {" + ", ".join(f"{v}u" for v in w) + "},")
+        e("};")
         e(f"constexpr int NSPRX = {len(jj)};")
         e(f"{qual} int kSpRxOff[NS + 1] = {{{', '.join(str(x) for x in off)}}};")
         e(f"{qual} int kSpRxJ[NSPRX] = {{{', '.join(str(x) for x in jj)}}};")
@@ -653,6 +677,8 @@ def gen_tables(m: Mechanism, space: str = "constant") -> str:
         e("  __device__ static int sprx_end(int k) { return kSpRxOff[k + 1]; }")
         e("  __device__ static int sprx_j(int e) { return kSpRxJ[e]; }")
         e("  __device__ static double sprx_nu(int e) { return kSpRxNu[e]; }")
+        e("  __device__ static const TabRxArr& rx_arr(int j) { return kRxArr[j]; }")
+        e("  __device__ static TabRxPk rx_pk(int j) { return kRxPk[j]; }")
         e("  static constexpr int JAC_TERMS = NJT;")
         e("  __device__ static unsigned jac_code(int c) { return kJacC[c]; }")
         e("  __device__ static unsigned jac_neg(int t) { return kJacNeg[t]; }")

@@ -232,3 +232,33 @@ def test_jacobian_program_replays_the_reaction_walk():
         np.testing.assert_allclose(B, A, rtol=1e-12, atol=0)
         assert set(np.nonzero(A)[0].tolist()) <= set(owner), "a nonzero entry has no lane"
         assert max(terms) <= 1.5 * np.mean(terms) + 20, (name, terms)
+
+
+def test_packed_reaction_records_match_the_reaction_table():
+    """The warp and lane-group RHS read each reaction through two packed records (kRxArr,
+    kRxPk); decoded, they must equal the fields of the FP64 reaction table entry by entry."""
+    import re
+    from pelelm_gb300.mech.codegen import gen_tables
+    for name in ("lidryer_syn", "drm19_syn", "gri_syn"):
+        txt = gen_tables(load_mechanism(name), "global")
+
+        def rows(nm):
+            body = re.search(nm + r"\[NR\] = \{\n(.*?)\n\};", txt, re.S).group(1)
+            return [r.strip().rstrip(",") for r in body.split("\n")]
+
+        def nums(row):
+            return [float(x.rstrip("uf")) for x in re.findall(r"-?[0-9][0-9.e+-]*u?", row)]
+
+        ref, arr, pk = rows("kReactionsD"), rows("kRxArr"), rows("kRxPk")
+        assert len(ref) == len(arr) == len(pk) > 0
+        for r, a, p in zip(ref, arr, pk):
+            f = nums(r)  # lnA beta mEaR kind rev nr np rs0 rs1 rs2 ps0 ps1 ps2 dnu tb troe
+            A = nums(a)
+            x, y, z, w = (int(v) for v in nums(p))
+            assert A[:3] == f[:3] and A[3] == 0.0 and w == 0
+            kind, rev, nr, np_ = x & 3, (x >> 2) & 1, (x >> 3) & 3, (x >> 5) & 3
+            dnu, tb, troe = ((x >> 7) & 15) - 8, ((x >> 11) & 2047) - 1, (x >> 22) - 1
+            assert [kind, rev, nr, np_] == f[3:7]
+            assert [dnu, tb, troe] == f[13:16]
+            assert [(y >> (10 * s)) & 1023 for s in range(nr)] == f[7:7 + nr]
+            assert [(z >> (10 * s)) & 1023 for s in range(np_)] == f[10:10 + np_]
