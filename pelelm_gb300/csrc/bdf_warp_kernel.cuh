@@ -220,8 +220,9 @@ __device__ __noinline__ WVec<M> warp_rhs(const WVec<M> yv, double* CS, double* G
 
 // Jacobian (equations of jac_table, mech_tables.cuh) and partial-pivot LU of I - gamma J in
 // shared memory, one warp cooperating; out of line like warp_rhs (called every few steps,
-// it would otherwise share the instruction cache with the step loop). False: singular.
-template <class M, class JR>
+// it would otherwise share the instruction cache with the step loop). False: singular. With
+// FACTOR false it stops after the Jacobian, which A then holds (the diagnostic entry point).
+template <class M, class JR, bool FACTOR = true>
 __device__ __noinline__ bool warp_setup(const WVec<M> yv, const double gamma, const double* FRC, JR* A,
                                         JR* XS, JR* RX, JR* TH, int* PIV) {
   using Tab = typename M::TabG;
@@ -515,7 +516,51 @@ __device__ __noinline__ bool warp_setup(const WVec<M> yv, const double gamma, co
     return true;
   };
   jacobian(yv.v);
-  return factor(gamma);
+  if constexpr (FACTOR) return factor(gamma);
+  else return true;
+}
+
+// (I - gamma J) x = b with the factors warp_setup left in A / PIV (trailing row swaps,
+// reciprocal pivots on the diagonal): one warp, rows over lanes, b distributed like the state
+// (element i in lane i mod 32) and overwritten with x; XS is the N-element staging vector.
+template <class M, class JR>
+__device__ __forceinline__ void warp_lu_solve(const JR* A, const int* PIV, JR* XS, double (&b)[(M::N + 31) / 32]) {
+  constexpr int N = M::N, R = (N + 31) / 32, LDA = N + 1;
+  const int lane = threadIdx.x & 31;
+  auto idx = [&](int r) { return lane + 32 * r; };
+#pragma unroll
+  for (int r = 0; r < R; ++r)
+    if (idx(r) < N) XS[idx(r)] = (JR)b[r];
+  __syncwarp();
+#pragma unroll 1
+  for (int k = 0; k < N; ++k) {
+    const int p = PIV[k];
+    if (p != k && lane == 0) { const JR tmp = XS[k]; XS[k] = XS[p]; XS[p] = tmp; }
+    __syncwarp();
+    const JR bk = XS[k];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int i = idx(r);
+      if (i > k && i < N) XS[i] -= A[i * LDA + k] * bk;
+    }
+    __syncwarp();
+  }
+#pragma unroll 1
+  for (int k = N - 1; k >= 0; --k) {
+    const JR xk = XS[k] * A[k * LDA + k];
+    __syncwarp();
+    if (lane == 0) XS[k] = xk;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int i = idx(r);
+      if (i < k) XS[i] -= A[i * LDA + k] * xk;
+    }
+    __syncwarp();
+  }
+#pragma unroll
+  for (int r = 0; r < R; ++r)
+    if (idx(r) < N) b[r] = (double)XS[idx(r)];
+  __syncwarp();
 }
 
 template <class M, class JR, int WPB>
@@ -572,41 +617,7 @@ __global__ void __launch_bounds__(WPB * 32, 1) bdf_warp_kernel(const ReactParams
   };
 
   // ---- analytic Jacobian into A (equations of jac_table, mech_tables.cuh), in type JR ----
-  auto solve = [&](double (&b)[R]) {
-#pragma unroll
-    for (int r = 0; r < R; ++r)
-      if (idx(r) < N) XS[idx(r)] = (JR)b[r];
-    __syncwarp();
-#pragma unroll 1
-    for (int k = 0; k < N; ++k) {
-      const int p = PIV[k];
-      if (p != k && lane == 0) { const JR tmp = XS[k]; XS[k] = XS[p]; XS[p] = tmp; }
-      __syncwarp();
-      const JR bk = XS[k];
-#pragma unroll
-      for (int r = 0; r < R; ++r) {
-        const int i = idx(r);
-        if (i > k && i < N) XS[i] -= A[i * LDA + k] * bk;
-      }
-      __syncwarp();
-    }
-#pragma unroll 1
-    for (int k = N - 1; k >= 0; --k) {
-      const JR xk = XS[k] * A[k * LDA + k];
-      __syncwarp();
-      if (lane == 0) XS[k] = xk;
-#pragma unroll
-      for (int r = 0; r < R; ++r) {
-        const int i = idx(r);
-        if (i < k) XS[i] -= A[i * LDA + k] * xk;
-      }
-      __syncwarp();
-    }
-#pragma unroll
-    for (int r = 0; r < R; ++r)
-      if (idx(r) < N) b[r] = (double)XS[idx(r)];
-    __syncwarp();
-  };
+  auto solve = [&](double (&b)[R]) { warp_lu_solve<M, JR>(A, PIV, XS, b); };
 
   for (;;) {
     // ---------------------------------------------- next cell (work stealing, one per warp)

@@ -10,6 +10,7 @@
 
 #include "../../include/pelelm_gb300.h"
 #include "bdf_group_kernel.cuh"
+#include "newton_matrix_kernel.cuh"
 #include "bdf_kernel.cuh"
 #include "bdf_warp_kernel.cuh"
 #include "point_kernels.cuh"
@@ -215,6 +216,7 @@ struct MechEntry {
   int (*hr_fn)(const pgb_box*, const pgb_array4*, const pgb_array4*, const pgb_array4*, cudaStream_t);
   LaunchFn group_mixed, group_fp64;  // group-per-cell BDF (argument: lanes per cell, 4 or 8)
   int (*group_cells_mixed)(int), (*group_cells_fp64)(int);  // cells per block for a group size
+  int (*newton_fn)(const pgb::NewtonMatrixParams&, int fp64, cudaStream_t);  // diagnostic
 };
 
 
@@ -260,6 +262,30 @@ int rates_entry(const pgb_box_view* v, const pgb_array4* out, cudaStream_t s) {
   pgb::rates_kernel<M><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(p);
   PGB_CUDA(cudaGetLastError());
   return 0;
+}
+
+// Newton matrix pieces of the warp / lane-group setup for a batch of states (diagnostic).
+template <class M, class JR>
+int launch_newton_matrix_jr(const pgb::NewtonMatrixParams& p, cudaStream_t s, int nsm) {
+  constexpr int smem = pgb::newton_matrix_smem<M, JR>();
+  if constexpr (smem > kMaxSmemPerBlock) {
+    return set_err("newton matrix: %d B of shared memory per cell exceed %d B", smem, kMaxSmemPerBlock);
+  } else {
+    auto kern = pgb::newton_matrix_kernel<M, JR>;
+    PGB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    const long long nb = std::min<long long>(p.ncell, (long long)nsm * 8);
+    kern<<<(unsigned)nb, 32, smem, s>>>(p);
+    PGB_CUDA(cudaGetLastError());
+    return 0;
+  }
+}
+template <class M>
+int newton_matrix_entry(const pgb::NewtonMatrixParams& p, int fp64, cudaStream_t s) {
+  if (p.ncell <= 0) return 0;
+  int dev = 0, nsm = 0;
+  PGB_CUDA(cudaGetDevice(&dev));
+  PGB_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  return fp64 ? launch_newton_matrix_jr<M, double>(p, s, nsm) : launch_newton_matrix_jr<M, float>(p, s, nsm);
 }
 
 template <class M>
@@ -315,7 +341,8 @@ int h2t_entry(const pgb_box_view* v, double tmin, double tmax, cudaStream_t s) {
       ::pgb_host::warp_wpb_choice<M>(0), ::pgb_host::warp_wpb_choice<M>(1),                  \
           ::pgb_host::warp_wpb_choice<M>(2), ::pgb_host::warp_wpb_choice<M>(3)               \
     }                                                                                        \
-    , ::pgb_host::heat_release_entry<M>, nullptr, nullptr, nullptr, nullptr                 \
+    , ::pgb_host::heat_release_entry<M>, nullptr, nullptr, nullptr, nullptr,                \
+        ::pgb_host::newton_matrix_entry<M>                                                   \
   }
 
 // Mechanisms whose cells also run group-per-cell (the 21-species size): all of the above plus
@@ -339,7 +366,7 @@ int h2t_entry(const pgb_box_view* v, double tmin, double tmax, cudaStream_t s) {
     }                                                                                        \
     , ::pgb_host::heat_release_entry<M>, ::pgb_host::launch_bdf_group<M, float>,             \
         ::pgb_host::launch_bdf_group<M, double>, ::pgb_host::group_cells_per_block<M, float>, \
-        ::pgb_host::group_cells_per_block<M, double>                                         \
+        ::pgb_host::group_cells_per_block<M, double>, ::pgb_host::newton_matrix_entry<M>     \
   }
 
 // Mechanisms too large for one cell per thread: warp-per-cell BDF, ReactorNull and T(h, Y) only.
@@ -354,7 +381,8 @@ int h2t_entry(const pgb_box_view* v, double tmin, double tmax, cudaStream_t s) {
       ::pgb_host::warp_wpb_choice<M>(0), ::pgb_host::warp_wpb_choice<M>(1),                  \
           ::pgb_host::warp_wpb_choice<M>(2), ::pgb_host::warp_wpb_choice<M>(3)               \
     }                                                                                        \
-    , ::pgb_host::heat_release_entry<M>, nullptr, nullptr, nullptr, nullptr                 \
+    , ::pgb_host::heat_release_entry<M>, nullptr, nullptr, nullptr, nullptr,                \
+        ::pgb_host::newton_matrix_entry<M>                                                   \
   }
 
 // Converts and validates one box view into its device descriptor; cell numbering of the box
