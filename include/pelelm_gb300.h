@@ -176,18 +176,20 @@ int pgb_reaction_rates(const char* mechanism, const pgb_box_view* view, const pg
 int pgb_heat_release(const char* mechanism, const pgb_box* box, const pgb_array4* T,
                      const pgb_array4* rhoYdot, const pgb_array4* hr, void* stream);
 
-/* Diagnostic: the Newton matrix pieces of the warp and lane-group BDF kernels for ncell states,
- * so a test can compare them with an independent implementation. No counterpart in the
- * reference (inside it these are CVODE's Jacobian and dense linear solve, cvode.solve_type =
- * denseAJ_direct, Exec/RegTests/FlameSheet/inputs.2d-regt:86-91). Device arrays, cell-major, CGS:
- * y [ncell][N] (rhoY, then T; N = NUM_SPECIES + 1), F [ncell][NUM_SPECIES] rhoY forcing, Fh
- * [ncell] rho h forcing, b [ncell][N]. Out: J [ncell][N][N] row-major (d ydot_i / d y_k, the
- * analytic Jacobian the kernels build), x [ncell][N] solving (I - gamma J) x = b through their
- * partial-pivot LU and triangular solves (NaN where the matrix is singular). fp64 = 0 runs the
- * FP32 Jacobian and LU of mixed precision. Stream ordered. */
-int pgb_newton_matrix(const char* mechanism, long long ncell, const double* y, const double* F,
-                      const double* Fh, double gamma, const double* b, int fp64, double* J, double* x,
-                      void* stream);
+/* Diagnostic: the Newton matrix pieces of the BDF kernels for ncell states, so a test can
+ * compare them with an independent implementation. No counterpart in the reference (inside it
+ * these are CVODE's Jacobian and dense linear solve, cvode.solve_type = denseAJ_direct,
+ * Exec/RegTests/FlameSheet/inputs.2d-regt:86-91). mapping 1: the warp and lane-group kernels
+ * (J and x); mapping 0: the cell-per-thread kernels (J only, x set to NaN; an error for
+ * mechanisms compiled without them). Device arrays, cell-major, CGS: y [ncell][N] (rhoY, then T;
+ * N = NUM_SPECIES + 1), F [ncell][NUM_SPECIES] rhoY forcing, Fh [ncell] rho h forcing, b
+ * [ncell][N]. Out: J [ncell][N][N] row-major (d ydot_i / d y_k, the analytic Jacobian the
+ * kernels build), x [ncell][N] solving (I - gamma J) x = b through their partial-pivot LU and
+ * triangular solves (NaN where the matrix is singular). fp64 = 0 runs the FP32 Jacobian and LU
+ * of mixed precision. Stream ordered. */
+int pgb_newton_matrix(const char* mechanism, int mapping, long long ncell, const double* y,
+                      const double* F, const double* Fh, double gamma, const double* b, int fp64,
+                      double* J, double* x, void* stream);
 
 /* T from (rho h, Y): the per-cell work of RhoH_to_Temp / getTfromHY (Source/PeleLM.cpp:8201-8287,
  * Source/PeleLM_K.H:508-529). MKS in: rhoY (view->rY), rhoH (view->rEner), T in/out (view->T).

@@ -80,8 +80,8 @@ EXPORTS = {
     "pgb_mlp_f32_to_bf16": (C.c_int, [_vp, _vp, C.c_longlong, _vp]),
     "pgb_mlp_dup_weight_bf16": (C.c_int, [_vp, C.c_int, C.c_int, _vp, C.c_int, _vp]),
     "pgb_mlp_split_rows_bf16": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _vp, C.c_int, C.c_int, _vp]),
-    "pgb_newton_matrix": (C.c_int, [C.c_char_p, C.c_longlong, _vp, _vp, _vp, C.c_double, _vp, C.c_int,
-                                    _vp, _vp, _vp]),
+    "pgb_newton_matrix": (C.c_int, [C.c_char_p, C.c_int, C.c_longlong, _vp, _vp, _vp, C.c_double, _vp,
+                                    C.c_int, _vp, _vp, _vp]),
     "pgb_react_boxes_noalloc": (C.c_int, [C.c_char_p, C.POINTER(BoxView), C.c_int, C.c_double,
                                           C.c_double, C.c_double, C.c_int, C.c_int, C.c_int, _vp,
                                           C.POINTER(Stats)]),

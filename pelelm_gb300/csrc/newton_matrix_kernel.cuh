@@ -1,11 +1,15 @@
-// Diagnostic kernel: the Newton matrix pieces of the warp and lane-group BDF kernels for a batch
-// of states, so a test can hold them against the oracle directly (the analytic Jacobian of
+// Diagnostic kernels: the Newton matrix pieces of the BDF kernels for a batch of states, so a
+// test can hold them against the oracle directly (the analytic Jacobian of
 // Source/PeleLM.cpp:5752's CVODE reactor, cvode.solve_type = denseAJ_direct, and its dense
-// solve). One warp per cell runs the production code: warp_setup without its factorization
-// gives J; warp_setup with it and warp_lu_solve give x solving (I - gamma J) x = b.
+// solve). Each runs the production code:
+//  * warp and lane-group kernels: one warp per cell; warp_setup without its factorization gives
+//    J, warp_setup with it and warp_lu_solve give x solving (I - gamma J) x = b;
+//  * cell-per-thread kernels: one thread per cell; the Jacobian call of their matrix setup
+//    (the generated M::jac, or jac_table for table-driven mechanisms) gives J.
 #ifndef PGB_NEWTON_MATRIX_KERNEL_CUH
 #define PGB_NEWTON_MATRIX_KERNEL_CUH
 
+#include "bdf_kernel.cuh"
 #include "bdf_warp_kernel.cuh"
 
 namespace pgb {
@@ -70,6 +74,40 @@ __global__ void __launch_bounds__(32) newton_matrix_kernel(const NewtonMatrixPar
       if (i < N) P.x[c * N + i] = ok ? b[r] : __longlong_as_double(0x7ff8000000000000LL);
     }
     __syncwarp();
+  }
+}
+
+// Shared bytes of one 32-thread block of the per-thread variant: each thread's J and
+// concentration scratch laid out [element][thread], as in the per-thread BDF kernel.
+template <class M, class JR>
+__host__ __device__ constexpr int newton_matrix_thread_smem() {
+  return 32 * (M::N * M::N + M::N) * (int)sizeof(JR);
+}
+
+template <class M, class JR>
+__global__ void __launch_bounds__(32) newton_matrix_thread_kernel(const NewtonMatrixParams P) {
+  constexpr int N = M::N, NS = M::NS;
+  extern __shared__ __align__(16) unsigned char tsmem[];
+  JR* Jt = reinterpret_cast<JR*>(tsmem) + threadIdx.x;  // element (i, k) at (i N + k) 32
+  JR* Ct = reinterpret_cast<JR*>(tsmem) + 32 * N * N + threadIdx.x;
+  for (long long c = (long long)blockIdx.x * 32 + threadIdx.x; c < P.ncell; c += (long long)gridDim.x * 32) {
+    double y[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) y[i] = P.y[c * N + i];
+    const double* F = P.F + c * NS;
+    LuAcc<JR> acc{Jt, N, 32};
+    if constexpr (M::JAC_TABLE) {
+      jac_table<typename M::Tab, JR>(y, [&](int k) -> double { return F[k]; }, P.Fh[c], acc,
+                                     [&](int k) -> JR& { return Ct[k * 32]; });
+    } else {
+      double Fl[NS];
+#pragma unroll
+      for (int i = 0; i < NS; ++i) Fl[i] = F[i];
+      M::template jac<JR>(y, Fl, P.Fh[c], acc);
+    }
+    for (int i = 0; i < N; ++i)
+      for (int k = 0; k < N; ++k) P.J[c * N * N + i * N + k] = (double)acc(i, k);
+    for (int i = 0; i < N; ++i) P.x[c * N + i] = __longlong_as_double(0x7ff8000000000000LL);
   }
 }
 

@@ -965,9 +965,9 @@ int pgb_heat_release(const char* mechanism, const pgb_box* box, const pgb_array4
   return m->hr_fn(box, T, rhoYdot, hr, static_cast<cudaStream_t>(stream));
 }
 
-int pgb_newton_matrix(const char* mechanism, long long ncell, const double* y, const double* F,
-                      const double* Fh, double gamma, const double* b, int fp64, double* J, double* x,
-                      void* stream) {
+int pgb_newton_matrix(const char* mechanism, int mapping, long long ncell, const double* y,
+                      const double* F, const double* Fh, double gamma, const double* b, int fp64,
+                      double* J, double* x, void* stream) {
   const MechEntry* m = find_mech(mechanism);
   if (!m) return set_err("unknown mechanism '%s'", mechanism ? mechanism : "(null)");
   if (ncell < 0) return set_err("newton_matrix: ncell must be >= 0");
@@ -975,7 +975,7 @@ int pgb_newton_matrix(const char* mechanism, long long ncell, const double* y, c
   if (!m->newton_fn) return set_err("the Newton matrix diagnostic is not compiled for mechanism '%s'", m->name);
   pgb::NewtonMatrixParams p;
   p.ncell = ncell; p.y = y; p.F = F; p.Fh = Fh; p.b = b; p.gamma = gamma; p.J = J; p.x = x;
-  return m->newton_fn(p, fp64, static_cast<cudaStream_t>(stream));
+  return m->newton_fn(p, mapping, fp64, static_cast<cudaStream_t>(stream));
 }
 
 int pgb_rhoh_to_temp(const char* mechanism, const pgb_box_view* view, double tmin, double tmax,

@@ -216,7 +216,7 @@ struct MechEntry {
   int (*hr_fn)(const pgb_box*, const pgb_array4*, const pgb_array4*, const pgb_array4*, cudaStream_t);
   LaunchFn group_mixed, group_fp64;  // group-per-cell BDF (argument: lanes per cell, 4 or 8)
   int (*group_cells_mixed)(int), (*group_cells_fp64)(int);  // cells per block for a group size
-  int (*newton_fn)(const pgb::NewtonMatrixParams&, int fp64, cudaStream_t);  // diagnostic
+  int (*newton_fn)(const pgb::NewtonMatrixParams&, int mapping, int fp64, cudaStream_t);  // diagnostic
 };
 
 
@@ -279,13 +279,36 @@ int launch_newton_matrix_jr(const pgb::NewtonMatrixParams& p, cudaStream_t s, in
     return 0;
   }
 }
-template <class M>
-int newton_matrix_entry(const pgb::NewtonMatrixParams& p, int fp64, cudaStream_t s) {
+template <class M, class JR>
+int launch_newton_matrix_thread_jr(const pgb::NewtonMatrixParams& p, cudaStream_t s, int nsm) {
+  constexpr int smem = pgb::newton_matrix_thread_smem<M, JR>();
+  if constexpr (smem > kMaxSmemPerBlock) {
+    return set_err("newton matrix: %d B of shared memory per block exceed %d B", smem, kMaxSmemPerBlock);
+  } else {
+    auto kern = pgb::newton_matrix_thread_kernel<M, JR>;
+    PGB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    const long long nb = std::min<long long>((p.ncell + 31) / 32, (long long)nsm * 8);
+    kern<<<(unsigned)nb, 32, smem, s>>>(p);
+    PGB_CUDA(cudaGetLastError());
+    return 0;
+  }
+}
+// mapping 1: warp / lane-group kernels; mapping 0: cell-per-thread kernels (THREAD: compiled)
+template <class M, bool THREAD>
+int newton_matrix_entry(const pgb::NewtonMatrixParams& p, int mapping, int fp64, cudaStream_t s) {
+  if (mapping != 0 && mapping != 1) return set_err("newton matrix: mapping must be 0 (per thread) or 1 (per warp)");
   if (p.ncell <= 0) return 0;
   int dev = 0, nsm = 0;
   PGB_CUDA(cudaGetDevice(&dev));
   PGB_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-  return fp64 ? launch_newton_matrix_jr<M, double>(p, s, nsm) : launch_newton_matrix_jr<M, float>(p, s, nsm);
+  if (mapping == 1)
+    return fp64 ? launch_newton_matrix_jr<M, double>(p, s, nsm) : launch_newton_matrix_jr<M, float>(p, s, nsm);
+  if constexpr (THREAD) {
+    return fp64 ? launch_newton_matrix_thread_jr<M, double>(p, s, nsm)
+                : launch_newton_matrix_thread_jr<M, float>(p, s, nsm);
+  } else {
+    return set_err("newton matrix: mechanism %s has no cell-per-thread kernels", M::NAME);
+  }
 }
 
 template <class M>
@@ -342,7 +365,7 @@ int h2t_entry(const pgb_box_view* v, double tmin, double tmax, cudaStream_t s) {
           ::pgb_host::warp_wpb_choice<M>(2), ::pgb_host::warp_wpb_choice<M>(3)               \
     }                                                                                        \
     , ::pgb_host::heat_release_entry<M>, nullptr, nullptr, nullptr, nullptr,                \
-        ::pgb_host::newton_matrix_entry<M>                                                   \
+        ::pgb_host::newton_matrix_entry<M, true>                                             \
   }
 
 // Mechanisms whose cells also run group-per-cell (the 21-species size): all of the above plus
@@ -366,7 +389,8 @@ int h2t_entry(const pgb_box_view* v, double tmin, double tmax, cudaStream_t s) {
     }                                                                                        \
     , ::pgb_host::heat_release_entry<M>, ::pgb_host::launch_bdf_group<M, float>,             \
         ::pgb_host::launch_bdf_group<M, double>, ::pgb_host::group_cells_per_block<M, float>, \
-        ::pgb_host::group_cells_per_block<M, double>, ::pgb_host::newton_matrix_entry<M>     \
+        ::pgb_host::group_cells_per_block<M, double>,                                        \
+        ::pgb_host::newton_matrix_entry<M, true>                                             \
   }
 
 // Mechanisms too large for one cell per thread: warp-per-cell BDF, ReactorNull and T(h, Y) only.
@@ -382,7 +406,7 @@ int h2t_entry(const pgb_box_view* v, double tmin, double tmax, cudaStream_t s) {
           ::pgb_host::warp_wpb_choice<M>(2), ::pgb_host::warp_wpb_choice<M>(3)               \
     }                                                                                        \
     , ::pgb_host::heat_release_entry<M>, nullptr, nullptr, nullptr, nullptr,                \
-        ::pgb_host::newton_matrix_entry<M>                                                   \
+        ::pgb_host::newton_matrix_entry<M, false>                                            \
   }
 
 // Converts and validates one box view into its device descriptor; cell numbering of the box

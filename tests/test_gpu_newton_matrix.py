@@ -11,7 +11,9 @@ that production code on a batch of states:
   (what the Newton iteration uses: rows of J far below FP32's range, where the FP32 path's
   clamped exponentials dominate, are negligible next to the identity);
 * x solving (I - gamma J) x = b: normwise backward error of the GPU solution on the GPU's own
-  matrix, at the working precision of each mode (FP64 LU, FP32 LU).
+  matrix, at the working precision of each mode (FP64 LU, FP32 LU);
+* the cell-per-thread kernels' Jacobian (the generated one of the 9-species mechanism, the
+  table-driven one of the 21-species mechanism) against the oracle the same way.
 """
 import numpy as np
 import pytest
@@ -31,15 +33,16 @@ def _states(cfgname, n):
     return cfg, cs, y, b
 
 
-def _gpu(torch, cfg, cs, y, b, fp64):
+def _gpu(torch, cfg, cs, y, b, fp64, mapping=1):
     n, N = y.shape
     dev = dict(device="cuda", dtype=torch.float64)
     ty, tF = torch.tensor(y, **dev), torch.tensor(cs.rYsrc, **dev)
     tFh, tb = torch.tensor(cs.rEsrc, **dev), torch.tensor(b, **dev)
     J = torch.empty((n, N, N), **dev)
     x = torch.empty((n, N), **dev)
-    rc = _lib.lib().pgb_newton_matrix(cfg.mech.encode(), n, ty.data_ptr(), tF.data_ptr(), tFh.data_ptr(),
-                                      GAMMA, tb.data_ptr(), int(fp64), J.data_ptr(), x.data_ptr(), None)
+    rc = _lib.lib().pgb_newton_matrix(cfg.mech.encode(), mapping, n, ty.data_ptr(), tF.data_ptr(),
+                                      tFh.data_ptr(), GAMMA, tb.data_ptr(), int(fp64), J.data_ptr(),
+                                      x.data_ptr(), None)
     assert rc == 0, _lib.last_error()
     torch.cuda.synchronize()
     return J.cpu().numpy(), x.cpu().numpy()
@@ -105,3 +108,37 @@ def test_fp32_jacobian_and_solve_of_mixed_precision(native_lib, cuda, cfgname, n
     print(f"{cfg.mech}: FP32 I - gamma J vs FP64 {worst:.2e} of row scale (p99 "
           f"{np.quantile(rel[representable], 0.99):.2e}; {np.sum(~representable)} of {n} beyond FP32 range), "
           f"solve backward error {be:.2e} (componentwise {_componentwise_error(J32, x32, b):.2e})")
+
+
+def _oracle_rel(om, y, cs, J):
+    worst = 0.0
+    for c in range(y.shape[0]):
+        Jo = om.jac(y[c], cs.rYsrc[c], cs.rEsrc[c])
+        worst = max(worst, float(np.max(np.abs(J[c] - Jo) / (np.abs(Jo).max(axis=1, keepdims=True) + 1e-300))))
+    return worst
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("cfgname,n", CASES[:2])
+def test_per_thread_jacobian_matches_the_oracle(native_lib, oracle_mod, cuda, cfgname, n):
+    torch = cuda
+    cfg, cs, y, b = _states(cfgname, n)
+    om = oracle_mod.OracleMech(mech_path(cfg.mech))
+    J64, x = _gpu(torch, cfg, cs, y, b, fp64=True, mapping=0)
+    assert np.isnan(x).all()  # the per-thread variant computes J only
+    worst = _oracle_rel(om, y, cs, J64)
+    assert worst <= 1e-9, f"{cfg.mech}: per-thread FP64 Jacobian differs from the oracle by {worst:.3e}"
+    J32, _ = _gpu(torch, cfg, cs, y, b, fp64=False, mapping=0)
+    eye = np.eye(J64.shape[1])[None]
+    M64, M32 = eye - GAMMA * J64, eye - GAMMA * J32
+    rel = float((np.abs(M32 - M64) / np.abs(M64).max(axis=2, keepdims=True)).max())
+    assert np.isfinite(J32).all() and rel <= 1e-4, f"{cfg.mech}: per-thread FP32 Newton matrix off by {rel:.3e}"
+    print(f"{cfg.mech}: per-thread FP64 J vs oracle {worst:.2e} of row scale; FP32 I - gamma J vs FP64 {rel:.2e}")
+
+
+@pytest.mark.gpu
+def test_per_thread_jacobian_refused_without_per_thread_kernels(native_lib, cuda):
+    torch = cuda
+    cfg, cs, y, b = _states("gri_1M", 32)
+    with pytest.raises(AssertionError, match="cell-per-thread"):
+        _gpu(torch, cfg, cs, y, b, fp64=True, mapping=0)
