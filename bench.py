@@ -632,7 +632,7 @@ WORKLOAD_TEXT = {
 # dram__bytes_write.sum of an ncu capture of a smaller launch of the same kernel, divided by its
 # cells; profiles/)
 TRAFFIC_PER_CELL = {("lidryer_syn", "thread"): 22.81e6 / 131072,
-                    ("drm19_syn", "group"): (12.618496e6 + 0.043264e6) / 32768,
+                    ("drm19_syn", "group"): (12.428544e6 + 0.0) / 32768,
                     ("drm19_syn", "warp"): (12.076800e6 + 0.017408e6) / 32768}
 KERNEL_OF_FAMILY = {"thread": "bdf_reactor_kernel", "warp": "bdf_warp_kernel", "group": "bdf_group_kernel"}
 
